@@ -1,0 +1,290 @@
+#!/usr/bin/env python
+"""Benchmark of the P-SV forward solver: Gcell-updates/s on the 2100 x 900
+grid (2000 x 800 inner cells + 50-cell Cerjan boundary), 5000 time steps,
+400 receivers, one dipping source, FP32 wave fields, seeded layered
+Gaussian-random medium (psvwave_gb300/workloads.py, c1).
+
+A step is one complete forward simulation (forward_simulate of shot 0, no
+snapshot storage): nx * nz * nt cell-updates. One cell-update is both
+half-steps at one grid point, counted over the full grid incl. boundary.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank advances its own copy of the model
+(independent shots of the same survey; no data-path collective), so the
+scaling is weak and `value` sums the ranks' cell-updates over the slowest
+rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-updates/s"
+BYTES_PER_CELL = {"stress_step": 48, "velocity_step": 36}  # FP32 algorithmic bytes per cell
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def cpu_baseline(params_fn, media, seconds=12.0):
+    """The oracle port (the reference's algorithm in C/OpenMP) on a bounded
+    sample of the workload: the same grid and medium, fewer time steps."""
+    from oracle import portbind
+
+    def run(n):
+        p = params_fn(nt=n)
+        p["snapshot_interval"] = n
+        o = portbind.OracleModel(params=p)
+        o.set_parameter_fields(*media)
+        t = time.perf_counter()
+        o.forward_simulate(0, False)
+        return time.perf_counter() - t, o.nx, o.nz
+
+    dt0, nx, nz = run(20)
+    cells = nx * nz
+    rate = cells * 20 / dt0
+    n = int(max(20, min(5000, seconds * rate / cells)))
+    n -= n % 10
+    dt, nx, nz = run(n)
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": cells * n / dt / 1e9, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "oracle port (C, OpenMP) forward on the c1 grid %dx%d and medium, "
+                      "%d of 5000 time steps, %.1f s" % (nx, nz, n, dt)}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    from psvwave_gb300 import workloads
+
+    media = workloads.c1_media()
+    samples = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(workloads.c1_params, media, seconds=5.0)
+        if i >= args.warmup:
+            samples.append(b["value"])
+            base = b
+    value = sum(samples) / len(samples)
+    base["value"] = value
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded layered medium)",
+            "config": {"workload": "c1: 2100x900 grid, nt=5000 (bounded sample per step), "
+                                   "400 receivers, forward only"},
+            "cpu_baseline": base,
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    import psvwave_gb300 as psv
+    from psvwave_gb300 import workloads
+
+    rank, local_rank, world = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+
+    params = workloads.c1_params()
+    media = workloads.c1_media(seed=1 + rank)
+    model = psv.fdModel.from_parameters(params, precision=args.precision, device=local_rank)
+    stream = torch.cuda.Stream(device=dev)
+    model.set_stream(stream.cuda_stream)
+    model.set_parameter_fields(*media)
+    cells = model.nx * model.nz
+    nt = model.nt
+    work = cells * nt
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        model.forward_simulate(0, False)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    barrier()
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)  # evict L2 between timed iterations (outside the timed span)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        model.forward_simulate(0, False)
+        e.record(stream)
+        e.synchronize()
+        total_ms += s.elapsed_time(e)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+
+    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = world * work * args.steps / (max_ms / 1e3) / 1e9
+
+    # End to end through the public API: host inputs from pinned memory,
+    # seismograms back to the host, every step.
+    pinned = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in media]
+    host_in = [p.numpy() for p in pinned]
+    for _ in range(max(1, args.warmup // 2)):
+        model.set_parameter_fields(*host_in)
+        model.forward_simulate(0, False)
+        model.get_synthetic_data()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        model.set_parameter_fields(*host_in)
+        model.forward_simulate(0, False)
+        ux, uz = model.get_synthetic_data()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = world * work * args.steps / float(t.item()) / 1e9
+    h2d = 3 * cells * 8
+    d2h = 2 * model.n_shots * model.nr * model.nt * 8
+
+    # Roofline of the dominant kernel: average launch duration from CUDA
+    # events around every launch, over 500 time steps.
+    per_step_ms, kernel_ms = model.profile_forward(0, 500)
+    dominant = max(kernel_ms, key=kernel_ms.get)
+    bpc = BYTES_PER_CELL[dominant] * (2 if args.precision == "fp64" else 1)
+    achieved = bpc * cells / (kernel_ms[dominant] / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": None, "bytes_per_launch": bpc * cells,
+                "kernel_ms": kernel_ms, "step_ms": per_step_ms}
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(workloads.c1_params, media)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32" else "f64",
+            "data": "synthetic (seeded layered + Gaussian-random medium)",
+            "config": {"workload": "c1: 2000x800 inner + 50-cell boundary (2100x900), nt=5000, "
+                                   "400 receivers, 1 source, forward only",
+                       "cells": cells, "nt": nt, "l2": "flushed between timed iterations",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": (2 * nt + 1) * args.steps,
+            "roofline": roofline,
+            "cpu_baseline": base,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

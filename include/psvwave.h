@@ -1,0 +1,236 @@
+/*
+ * psvwave.h -- C ABI of psvwave_gb300, a GB300 (sm_103a) implementation of
+ * psvWave's P-SV finite-difference solver (larsgeb/psvWave).
+ *
+ * Each entry point replaces one member of the reference's `fdModel` class
+ * (src/fdModel.h, src/fdModel.cpp) or of its Python binding
+ * (src/psvWave.cpp); the citation beside each declaration names it.
+ *
+ * Conventions
+ *  - Every function returns PSV_OK (0) or a PSV_ERR_* code; the message of
+ *    the last failure on the calling thread is psv_last_error(). No C++
+ *    exception crosses this boundary.
+ *  - Host arrays are double precision, C-contiguous, in the reference's
+ *    layouts: grids [nx][nz] with z fastest (src/contiguous_arrays.cpp:43-50),
+ *    receiver data [n_shots][nr][nt], snapshots [n_shots][snapshots][nx][nz].
+ *  - The wave fields are advanced in the precision chosen at creation:
+ *    PSV_FP32 (production) or PSV_FP64 (the reference's own precision,
+ *    bit-identical to it). Seismograms, misfit and kernel sums are FP64 in
+ *    both modes.
+ *  - Calls on one model are not thread-safe (the reference shares its fields
+ *    between calls the same way). Distinct models are independent.
+ *  - Device work is ordered on the model's CUDA stream; calls that hand data
+ *    back to the host synchronise that stream.
+ */
+#ifndef PSVWAVE_H
+#define PSVWAVE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PSVWAVE_ABI_VERSION 1
+
+enum psv_status {
+  PSV_OK = 0,
+  PSV_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument in the reference */
+  PSV_ERR_LENGTH = 2,           /* std::length_error in the reference */
+  PSV_ERR_IO = 3,               /* file missing / wrong amount of data */
+  PSV_ERR_CUDA = 4,             /* CUDA runtime failure */
+  PSV_ERR_NUMERIC = 5,          /* non-finite wave field detected */
+  PSV_ERR_INTERNAL = 6
+};
+
+enum psv_precision { PSV_FP32 = 0, PSV_FP64 = 1 };
+
+typedef struct psv_model psv_model;
+
+/* Scalar description of a model: the read-only attributes of the Python
+ * class (src/psvWave.cpp:499-588) plus the configuration it was built from. */
+typedef struct psv_info {
+  int nt, nx, nz, nx_inner, nz_inner, nx_inner_boundary, nz_inner_boundary;
+  int np_boundary, n_shots, n_sources, nr, snapshot_interval, snapshots;
+  int nx_free_parameters, nz_free_parameters, free_parameters;
+  int basis_gridpoints_x, basis_gridpoints_z;
+  int precision, device;
+  double dt, dx, dz, np_factor, peak_frequency, alpha, delay_cycles_per_shot;
+  double source_timeshift, scalar_rho, scalar_vp, scalar_vs, misfit;
+} psv_info;
+
+/* Explicit-parameter description of a model; the arguments of the
+ * reference's second constructor (src/fdModel.h:50-64). Source and receiver
+ * indices are inner-grid indices (the absorbing boundary is added, as
+ * src/fdModel.cpp:197-212 does). Shots are given in CSR form:
+ * shot_sources[shot_offsets[s] .. shot_offsets[s+1]) fire in shot s. */
+typedef struct psv_params {
+  int nt, nx_inner, nz_inner, nx_inner_boundary, nz_inner_boundary;
+  double dx, dz, dt;
+  int np_boundary;
+  double np_factor, scalar_rho, scalar_vp, scalar_vs;
+  int npx, npz;
+  double peak_frequency, source_timeshift, delay_cycles_per_shot;
+  int n_sources, n_shots;
+  const int *ix_sources, *iz_sources;
+  const double *moment_angles;
+  const int *shot_offsets, *shot_sources;
+  int nr;
+  const int *ix_receivers, *iz_receivers;
+  int snapshot_interval;
+  const char *observed_data_folder, *stf_folder;
+} psv_params;
+
+/* ---- library ---------------------------------------------------------- */
+int psv_abi_version(void);
+const char *psv_last_error(void);
+/* Number of CUDA devices visible; 0 when none. */
+int psv_device_count(int *count);
+
+/* Parses and validates a configuration file (the reference's INI reading,
+ * src/fdModel.cpp:470-523, and checks, src/fdModel.cpp:390-468) without
+ * touching a GPU; fills `out` with precision = device = -1 and misfit = 0. */
+int psv_config_info(const char *path, psv_info *out);
+
+/* ---- construction ----------------------------------------------------- */
+/* fdModel(const char *configuration_file) -- src/fdModel.cpp:16-27,470-523;
+ * Python: fdModel(configuration_file_path) -- src/psvWave.cpp:465-471. */
+int psv_create_from_ini(const char *path, int precision, int device, psv_model **out);
+/* fdModel(nt, nx_inner, ...) -- src/fdModel.cpp:29-62. */
+int psv_create(const psv_params *params, int precision, int device, psv_model **out);
+/* fdModel(const fdModel&) -- src/fdModel.cpp:64-97; Python copy() --
+ * src/psvWave.cpp:421-425. Deep copy incl. fields, data, kernels, snapshots. */
+int psv_clone(const psv_model *m, psv_model **out);
+/* ~fdModel() -- src/fdModel.cpp:99-137. Accepts NULL. */
+int psv_destroy(psv_model *m);
+int psv_get_info(const psv_model *m, psv_info *out);
+/* which_source_to_fire_in_which_shot (src/psvWave.cpp:586-588) in CSR form:
+ * offsets[n_shots+1], sources[n_sources]. */
+int psv_get_shot_sources(const psv_model *m, int *offsets, int *sources);
+/* Folders named by [output] (src/fdModel.cpp:517-518); buffers of `cap` bytes. */
+int psv_get_folders(const psv_model *m, char *observed, char *stf, size_t cap);
+
+/* ---- simulation ------------------------------------------------------- */
+/* forward_simulate -- src/fdModel.cpp:526-787; Python binding
+ * src/psvWave.cpp:112-158,476-498. `output_wavefields` writes
+ * snapshots/vx%05d.txt and vz%05d.txt every 10 steps (src/fdModel.cpp:753-776). */
+int psv_forward_simulate(psv_model *m, int i_shot, int store_fields, int verbose,
+                         int output_wavefields);
+/* adjoint_simulate -- src/fdModel.cpp:789-969; src/psvWave.cpp:160-205,634-650. */
+int psv_adjoint_simulate(psv_model *m, int i_shot, int verbose);
+/* calculate_l2_misfit -- src/fdModel.cpp:1128-1145. `misfit` may be NULL. */
+int psv_calculate_l2_misfit(psv_model *m, double *misfit);
+/* calculate_l2_adjoint_sources -- src/fdModel.cpp:1147-1162. */
+int psv_calculate_l2_adjoint_sources(psv_model *m);
+/* reset_kernels -- src/fdModel.cpp:1310-1324. */
+int psv_reset_kernels(psv_model *m);
+/* map_kernels_to_velocity -- src/fdModel.cpp:1164-1183. */
+int psv_map_kernels_to_velocity(psv_model *m);
+/* run_model(verbose, simulate_adjoint) -- src/fdModel.cpp:1291-1308: every
+ * shot forward with storage, misfit, and (if simulate_adjoint) adjoint
+ * sources, kernel reset, every shot adjoint and the velocity mapping. This is
+ * one FWI gradient ("compute_gradients"). */
+int psv_run_model(psv_model *m, int verbose, int simulate_adjoint);
+/* update_from_velocity -- src/fdModel.cpp:1034-1051. */
+int psv_update_from_velocity(psv_model *m);
+
+/* ---- model, data and kernel transfer (host FP64 arrays) --------------- */
+/* get_parameter_fields / set_parameter_fields -- src/psvWave.cpp:248-297
+ * (set recomputes the Lame fields). */
+int psv_get_parameter_fields(psv_model *m, double *vp, double *vs, double *rho);
+int psv_set_parameter_fields(psv_model *m, const double *vp, const double *vs,
+                             const double *rho);
+/* load_model(de, vp, vs, verbose) -- src/fdModel.cpp:1185-1289: nx*nz
+ * whitespace-separated values per file, ix-major. */
+int psv_load_model(psv_model *m, const char *de_path, const char *vp_path,
+                   const char *vs_path, int verbose);
+/* get_kernels -- src/psvWave.cpp:299-306: (vp, vs, rho) velocity kernels. */
+int psv_get_kernels(psv_model *m, double *vp_k, double *vs_k, double *rho_k);
+/* The Lame-basis kernels (lambda, mu, density) the adjoint accumulates
+ * (src/fdModel.h:224-226). */
+int psv_get_lame_kernels(psv_model *m, double *lambda_k, double *mu_k, double *rho_k);
+/* get/set_synthetic_data, get/set_observed_data -- src/psvWave.cpp:308-322,
+ * 389-457. */
+int psv_get_synthetic_data(psv_model *m, double *ux, double *uz);
+int psv_set_synthetic_data(psv_model *m, const double *ux, const double *uz);
+int psv_get_observed_data(psv_model *m, double *ux, double *uz);
+int psv_set_observed_data(psv_model *m, const double *ux, const double *uz);
+/* The adjoint sources a_stf_ux/uz (src/fdModel.h:246-247). */
+int psv_get_adjoint_sources(psv_model *m, double *ux, double *uz);
+/* get_snapshots -- src/psvWave.cpp:90-97: the five stored forward fields
+ * vx, vz, txx, tzz, txz of all shots. Any pointer may be NULL to skip it. */
+int psv_get_snapshots(psv_model *m, double *vx, double *vz, double *txx, double *tzz,
+                      double *txz);
+/* The current wave fields vx, vz, txx, tzz, txz (src/fdModel.h:209-213). */
+int psv_get_wavefields(psv_model *m, double *vx, double *vz, double *txx, double *tzz,
+                       double *txz);
+/* The source time functions [n_sources][nt] (src/fdModel.h:240), the moment
+ * tensors [n_sources][2][2] (src/fdModel.h:241) and the taper [nx][nz]
+ * (src/fdModel.h:236). */
+int psv_get_stf(psv_model *m, double *stf);
+int psv_get_moment(psv_model *m, double *moment);
+int psv_get_taper(psv_model *m, double *taper);
+
+/* get_model_vector / set_model_vector / get_gradient_vector --
+ * src/fdModel.cpp:1358-1515; vectors of length free_parameters. */
+int psv_get_model_vector(psv_model *m, double *out);
+int psv_set_model_vector(psv_model *m, const double *in);
+int psv_get_gradient_vector(psv_model *m, double *out);
+/* load_vector(path, verbose) -- src/fdModel.cpp:1517-1572: reads
+ * 3*nx_free*nz_free values (the unblocked size, as the reference does). */
+int psv_load_vector(psv_model *m, const char *path, int verbose, double *out);
+
+/* get_sources / get_receivers -- src/psvWave.cpp:324-387. */
+int psv_get_sources(psv_model *m, int in_units, int include_boundary, double *x, double *z);
+int psv_get_receivers(psv_model *m, int in_units, int include_boundary, double *x,
+                      double *z);
+/* get_coordinates -- src/psvWave.cpp:207-246. */
+int psv_get_coordinates(psv_model *m, int in_units, double *ix, double *iz);
+/* get_extent -- src/psvWave.cpp:99-110: out[4] = xmin, xmax, zmin, zmax. */
+int psv_get_extent(psv_model *m, int include_boundary, double *out4);
+
+/* ---- text I/O --------------------------------------------------------- */
+/* write_receivers(prefix) -- src/fdModel.cpp:971-1006. */
+int psv_write_receivers(psv_model *m, const char *prefix);
+/* load_receivers(verbose) -- src/fdModel.cpp:1053-1126. */
+int psv_load_receivers(psv_model *m, int verbose);
+/* write_sources -- src/fdModel.cpp:1008-1032. */
+int psv_write_sources(psv_model *m);
+/* write_kernels -- src/fdModel.cpp:1326-1356. */
+int psv_write_kernels(psv_model *m);
+
+/* ---- device-side interface (PyTorch layer) ----------------------------- */
+/* Order the model's device work on `stream` (a cudaStream_t; NULL = the
+ * model's own stream). */
+int psv_set_stream(psv_model *m, void *stream);
+/* Make forward/adjoint return without waiting for the GPU (1) or wait, as
+ * the reference's calls do (0, the default). */
+int psv_set_async(psv_model *m, int async_calls);
+int psv_synchronize(psv_model *m);
+/* Parameter fields from device FP64 buffers [nx][nz]. */
+int psv_set_parameter_fields_device(psv_model *m, const double *vp, const double *vs,
+                                    const double *rho);
+/* Observed data from device FP64 buffers [n_shots][nr][nt]. */
+int psv_set_observed_data_device(psv_model *m, const double *ux, const double *uz);
+/* Copy the synthetic data / velocity kernels into device FP64 buffers. */
+int psv_get_synthetic_data_device(psv_model *m, double *ux, double *uz);
+int psv_get_kernels_device(psv_model *m, double *vp_k, double *vs_k, double *rho_k);
+/* Bytes of device memory the model holds. */
+int psv_device_bytes(const psv_model *m, size_t *bytes);
+
+/* ---- measurement -------------------------------------------------------- */
+/* Runs the first n_steps forward time steps of `i_shot` (no storage) with a
+ * CUDA event around every kernel launch on the model's stream, and reports
+ * the average device time per time step (*per_step_ms) and per launch of
+ * each of the step's kernels (kernel_ms[k], in launch order; names from
+ * psv_step_kernel_name). *n_kernels receives the launches per step. Has no
+ * counterpart in the reference (which times with omp_get_wtime only,
+ * src/fdModel.cpp:545-549). */
+int psv_profile_forward(psv_model *m, int i_shot, int n_steps, double *per_step_ms,
+                        double *kernel_ms, int max_kernels, int *n_kernels);
+const char *psv_step_kernel_name(int k);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PSVWAVE_H */

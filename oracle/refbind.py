@@ -99,6 +99,10 @@ class RefModel:
         _load().ref_scalars(self._h, out)
         return dict(zip(SCALAR_FIELDS, list(out)))
 
+    @property
+    def misfit(self):
+        return self.scalars()["misfit"]
+
     def array(self, name):
         shapes = {
             "grid": (self.nx, self.nz),

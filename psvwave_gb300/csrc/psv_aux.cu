@@ -1,0 +1,103 @@
+// FP64 reductions and point-wise maps on receiver data and kernels.
+#include <cuda_runtime.h>
+
+#include "psv_solver.hpp"
+
+namespace psv {
+namespace {
+
+constexpr int kReduceThreads = 256;
+
+// Per-block partial sums of 0.5 dt (obs - syn)^2 over both components
+// (src/fdModel.cpp:1128-1145), in a fixed order.
+__global__ void misfit_partial(size_t n, double dt, const double *ou, const double *su,
+                               const double *oz, const double *sz, double *partials) {
+  __shared__ double acc[kReduceThreads];
+  double s = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double a = ou[i] - su[i], b = oz[i] - sz[i];
+    s += 0.5 * dt * (a * a);
+    s += 0.5 * dt * (b * b);
+  }
+  acc[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = kReduceThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) acc[threadIdx.x] += acc[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+
+__global__ void sum_partials(int n, const double *partials, double *out) {
+  __shared__ double acc[kReduceThreads];
+  double s = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partials[i];
+  acc[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = kReduceThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) acc[threadIdx.x] += acc[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = acc[0];
+}
+
+// a = syn - obs (src/fdModel.cpp:1147-1162).
+__global__ void residual(size_t n, const double *su, const double *ou, const double *sz,
+                         const double *oz, double *au, double *az) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    au[i] = su[i] - ou[i];
+    az[i] = sz[i] - oz[i];
+  }
+}
+
+// Lame -> velocity kernels with b = 1 / rho (src/fdModel.cpp:1164-1183).
+__global__ void lame_to_velocity(size_t n, const double *vp, const double *vs,
+                                 const double *rho, const double *kl, const double *km,
+                                 const double *kr, double *kvp, double *kvs, double *krv) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double b = 1.0 / rho[i];
+    const double p = vp[i], s = vs[i], l = kl[i], m = km[i];
+    kvp[i] = 2 * p * l / b;
+    kvs[i] = (2 * s * m - 4 * s * l) / b;
+    krv[i] = kr[i] + (p * p - 2 * s * s) * l + s * s * m;
+  }
+}
+
+unsigned blocks_for(size_t n) {
+  size_t b = (n + 255) / 256;
+  if (b > 4096) b = 4096;
+  if (b == 0) b = 1;
+  return static_cast<unsigned>(b);
+}
+
+}  // namespace
+
+cudaError_t misfit_l2(size_t n, double dt, const double *obs_ux, const double *syn_ux,
+                      const double *obs_uz, const double *syn_uz, double *partials,
+                      int n_partials, double *out, cudaStream_t s) {
+  misfit_partial<<<n_partials, kReduceThreads, 0, s>>>(n, dt, obs_ux, syn_ux, obs_uz, syn_uz,
+                                                       partials);
+  sum_partials<<<1, kReduceThreads, 0, s>>>(n_partials, partials, out);
+  return cudaGetLastError();
+}
+
+cudaError_t adjoint_sources_l2(size_t n, const double *syn_ux, const double *obs_ux,
+                               const double *syn_uz, const double *obs_uz, double *a_ux,
+                               double *a_uz, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  residual<<<blocks_for(n), 256, 0, s>>>(n, syn_ux, obs_ux, syn_uz, obs_uz, a_ux, a_uz);
+  return cudaGetLastError();
+}
+
+cudaError_t map_kernels(size_t n, const double *vp, const double *vs, const double *rho,
+                        const double *k_lam, const double *k_mu, const double *k_rho,
+                        double *vp_k, double *vs_k, double *rho_k, cudaStream_t s) {
+  lame_to_velocity<<<blocks_for(n), 256, 0, s>>>(n, vp, vs, rho, k_lam, k_mu, k_rho, vp_k,
+                                                 vs_k, rho_k);
+  return cudaGetLastError();
+}
+
+}  // namespace psv

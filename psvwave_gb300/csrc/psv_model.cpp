@@ -1,0 +1,1006 @@
+// Host orchestration of one P-SV model: setup tables, device memory, the
+// calls of the reference's fdModel API (src/fdModel.cpp), and text I/O.
+#include "psv_model.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <limits>
+#include <sstream>
+
+#include "../../include/psvwave.h"
+
+namespace psv {
+
+namespace {
+
+// The reference's degrees-to-radians constant (src/fdModel.cpp:14) and the
+// M_PI its Ricker wavelet uses (src/fdModel.cpp:227).
+constexpr double kRefPi = 3.14159265;
+constexpr double kMPi = 3.14159265358979323846;
+
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    cudaGetDevice(&prev_);
+    if (prev_ != device) cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    restore_ = prev_ != device;
+  }
+  ~DeviceGuard() {
+    if (restore_) cudaSetDevice(prev_);
+  }
+
+ private:
+  int prev_ = 0;
+  bool restore_ = false;
+};
+
+std::string pad5(int n) {
+  std::ostringstream ss;
+  ss << std::setw(5) << std::setfill('0') << n;
+  return ss.str();
+}
+
+}  // namespace
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(PSV_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+DeviceBuffer::~DeviceBuffer() { release(); }
+
+void DeviceBuffer::allocate(size_t bytes) {
+  release();
+  if (bytes == 0) bytes = 16;
+  cuda_check(cudaMalloc(&ptr_, bytes), "cudaMalloc");
+  bytes_ = bytes;
+  cuda_check(cudaMemset(ptr_, 0, bytes), "cudaMemset");
+}
+
+void DeviceBuffer::release() {
+  if (ptr_) cudaFree(ptr_);
+  ptr_ = nullptr;
+  bytes_ = 0;
+}
+
+// ---------------------------------------------------------------- setup --
+
+Model::Model(const Config &cfg, int precision, int device)
+    : cfg_(cfg), geo_(validate(cfg)), prec_(precision), device_(device) {
+  if (prec_ != PSV_FP32 && prec_ != PSV_FP64)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "precision must be PSV_FP32 or PSV_FP64");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    throw Error(PSV_ERR_CUDA, "no CUDA device is available");
+  }
+  if (device_ < 0 || device_ >= count)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "CUDA device index out of range");
+  DeviceGuard guard(device_);
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  build_tables();
+  allocate();
+  // Homogeneous background medium (src/fdModel.cpp:249-261).
+  std::vector<double> v(grid_size());
+  const double scal[3] = {cfg_.scalar_vp, cfg_.scalar_vs, cfg_.scalar_rho};
+  DeviceBuffer *dst[3] = {&vp_, &vs_, &rho_};
+  for (int k = 0; k < 3; ++k) {
+    std::fill(v.begin(), v.end(), scal[k]);
+    cuda_check(cudaMemcpy(dst[k]->get(), v.data(), v.size() * sizeof(double),
+                          cudaMemcpyHostToDevice),
+               "upload medium");
+  }
+  update_from_velocity();
+  build_plans();
+  synchronize();
+}
+
+Model::Model(const Model &o)
+    : cfg_(o.cfg_), geo_(o.geo_), prec_(o.prec_), device_(o.device_), async_(o.async_),
+      misfit_(o.misfit_) {
+  DeviceGuard guard(device_);
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  build_tables();
+  allocate();
+  build_plans();
+  const_cast<Model &>(o).synchronize();
+  auto copy = [&](DeviceBuffer &d, const DeviceBuffer &s) {
+    if (!s.get()) return;
+    if (d.bytes() != s.bytes()) d.allocate(s.bytes());
+    cuda_check(cudaMemcpy(d.get(), s.get(), s.bytes(), cudaMemcpyDeviceToDevice), "clone");
+  };
+  for (int k = 0; k < 5; ++k) copy(fields_[k], o.fields_[k]);
+  copy(lm_, o.lm_);
+  copy(la_, o.la_);
+  copy(mu_, o.mu_);
+  copy(b_, o.b_);
+  copy(vp_, o.vp_);
+  copy(vs_, o.vs_);
+  copy(rho_, o.rho_);
+  for (int k = 0; k < 5; ++k) copy(accu_[k], o.accu_[k]);
+  for (int k = 0; k < 2; ++k) {
+    copy(rtf_[k], o.rtf_[k]);
+    copy(rtf_true_[k], o.rtf_true_[k]);
+    copy(a_stf_[k], o.a_stf_[k]);
+  }
+  copy(rec_raw_, o.rec_raw_);
+  for (int k = 0; k < 3; ++k) {
+    copy(klame_[k], o.klame_[k]);
+    copy(kvel_[k], o.kvel_[k]);
+  }
+}
+
+Model::~Model() {
+  DeviceGuard guard(device_);
+  if (stream_) {
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+  }
+}
+
+void Model::build_tables() {
+  const int np = cfg_.np_boundary;
+  // Source/receiver positions in the padded grid (src/fdModel.cpp:197-212).
+  ix_src_.clear();
+  iz_src_.clear();
+  ix_rec_.clear();
+  iz_rec_.clear();
+  for (int i = 0; i < cfg_.n_sources; ++i) {
+    ix_src_.push_back(cfg_.ix_sources[i] + np);
+    iz_src_.push_back(cfg_.iz_sources[i] + np);
+  }
+  for (int i = 0; i < cfg_.nr; ++i) {
+    ix_rec_.push_back(cfg_.ix_receivers[i] + np);
+    iz_rec_.push_back(cfg_.iz_receivers[i] + np);
+  }
+  // Ricker wavelets, each delayed by delay_cycles_per_shot periods per
+  // position in its shot (src/fdModel.cpp:215-231).
+  const int nt = cfg_.nt;
+  stf_.assign(static_cast<size_t>(cfg_.n_sources) * nt, 0.0);
+  for (const auto &shot : cfg_.shots) {
+    for (size_t pos = 0; pos < shot.size(); ++pos) {
+      const int src = shot[pos];
+      for (int it = 0; it < nt; ++it) {
+        const double t = static_cast<double>(static_cast<unsigned>(it)) * cfg_.dt;
+        const double f = 1.0 / geo_.alpha;
+        const double shifted =
+            t - 1.4 / f - cfg_.delay_cycles_per_shot * static_cast<int>(pos) / f;
+        const double a = kMPi * f * shifted;
+        stf_[static_cast<size_t>(src) * nt + it] = (1 - 2 * (a * a)) * std::exp(-(a * a));
+      }
+    }
+  }
+  // Moment tensors of reverse faults rotated by their dip (src/fdModel.cpp:234-246).
+  moment_.assign(static_cast<size_t>(cfg_.n_sources) * 4, 0.0);
+  for (int i = 0; i < cfg_.n_sources; ++i) {
+    const double r = cfg_.moment_angles[i] * kRefPi / 180.0;
+    moment_[4 * i + 0] = std::cos(r) * 1e15;
+    moment_[4 * i + 1] = -std::sin(r) * 1e15;
+    moment_[4 * i + 2] = -std::sin(r) * 1e15;
+    moment_[4 * i + 3] = -std::cos(r) * 1e15;
+  }
+  // Cerjan taper as a function of the nested-frame count c in [0, np]
+  // (src/fdModel.cpp:263-298): exp(-(np_factor (np - c))^2).
+  taper_tab_.assign(static_cast<size_t>(np) + 1, 1.0);
+  for (int c = 0; c <= np; ++c) {
+    const double a = cfg_.np_factor * (static_cast<double>(np) - static_cast<double>(c));
+    taper_tab_[c] = std::exp(-(a * a));
+  }
+}
+
+void Model::allocate() {
+  const size_t g = grid_size(), e = elem(), d = data_size();
+  for (auto &f : fields_) f.allocate(g * e);
+  lm_.allocate(g * e);
+  la_.allocate(g * e);
+  mu_.allocate(g * e);
+  b_.allocate(g * e);
+  vp_.allocate(g * sizeof(double));
+  vs_.allocate(g * sizeof(double));
+  rho_.allocate(g * sizeof(double));
+  for (int k = 0; k < 2; ++k) {
+    rtf_[k].allocate(d * sizeof(double));
+    rtf_true_[k].allocate(d * sizeof(double));
+    a_stf_[k].allocate(d * sizeof(double));
+  }
+  rec_raw_.allocate(2 * static_cast<size_t>(cfg_.nr) * cfg_.nt * e);
+  rec_cell_.allocate(static_cast<size_t>(cfg_.nr) * sizeof(int));
+  for (auto &k : klame_) k.allocate(g * sizeof(double));
+  for (auto &k : kvel_) k.allocate(g * sizeof(double));
+  partials_.allocate(kPartials * sizeof(double));
+  scalar_.allocate(sizeof(double));
+  stf_d_.allocate(stf_.size() * sizeof(double));
+  if (!stf_.empty())
+    cuda_check(cudaMemcpy(stf_d_.get(), stf_.data(), stf_.size() * sizeof(double),
+                          cudaMemcpyHostToDevice),
+               "upload stf");
+  std::vector<int> cells(cfg_.nr);
+  for (int r = 0; r < cfg_.nr; ++r) cells[r] = ix_rec_[r] * geo_.nz + iz_rec_[r];
+  if (cfg_.nr)
+    cuda_check(cudaMemcpy(rec_cell_.get(), cells.data(), cells.size() * sizeof(int),
+                          cudaMemcpyHostToDevice),
+               "upload receivers");
+  taper_tab_d_.allocate(taper_tab_.size() * e);
+  if (prec_ == PSV_FP64) {
+    cuda_check(cudaMemcpy(taper_tab_d_.get(), taper_tab_.data(),
+                          taper_tab_.size() * sizeof(double), cudaMemcpyHostToDevice),
+               "upload taper");
+  } else {
+    std::vector<float> t(taper_tab_.begin(), taper_tab_.end());
+    cuda_check(cudaMemcpy(taper_tab_d_.get(), t.data(), t.size() * sizeof(float),
+                          cudaMemcpyHostToDevice),
+               "upload taper");
+  }
+}
+
+// Injection terms in the reference's serial order, grouped by point.
+void Model::build_plans() {
+  const int nz = geo_.nz, n_shots = cfg_.n_shots;
+  const double dx = cfg_.dx, dz = cfg_.dz;
+  const double dx4 = dx * dx * dx * dx, dz4 = dz * dz * dz * dz;
+  plans_.assign(n_shots + 1, InjPlan());
+  plan_terms_.clear();
+  plan_maps_.clear();
+  plan_terms_.resize(n_shots + 1);
+  plan_maps_.resize(n_shots + 1);
+  for (int p = 0; p <= n_shots; ++p) {
+    std::vector<InjTerm> terms;
+    auto add = [&](int cell, int field, int index, int kind, double coef, double div) {
+      terms.push_back(InjTerm{cell, field, index, kind, coef, div});
+    };
+    if (p < n_shots) {
+      // src/fdModel.cpp:681-751
+      for (int s : cfg_.shots[p]) {
+        const int c = ix_src_[s] * nz + iz_src_[s];
+        const double *M = &moment_[4 * s];
+        const double q01 = 0.25 * M[1], q10 = 0.25 * M[2];
+        add(c - nz, 0, s, 0, -M[0], dx4);
+        add(c, 0, s, 0, M[0], dx4);
+        add(c - 1, 1, s, 0, -M[3], dz4);
+        add(c, 1, s, 0, M[3], dz4);
+        add(c - nz + 1, 0, s, 0, q01, dx4);
+        add(c + 1, 0, s, 0, q01, dx4);
+        add(c - nz - 1, 0, s, 0, -q01, dx4);
+        add(c - 1, 0, s, 0, -q01, dx4);
+        add(c + nz - 1, 1, s, 0, q10, dz4);
+        add(c + nz, 1, s, 0, q10, dz4);
+        add(c - nz - 1, 1, s, 0, -q10, dz4);
+        add(c - nz, 1, s, 0, -q10, dz4);
+      }
+    } else {
+      // src/fdModel.cpp:951-958
+      for (int r = 0; r < cfg_.nr; ++r) {
+        const int c = ix_rec_[r] * nz + iz_rec_[r];
+        add(c, 0, r, 1, 0.0, dx * dz);
+        add(c, 1, r, 1, 0.0, dx * dz);
+      }
+    }
+    std::stable_sort(terms.begin(), terms.end(),
+                     [](const InjTerm &a, const InjTerm &b) { return a.cell < b.cell; });
+    InjPlan plan;
+    plan.n = static_cast<int>(terms.size());
+    if (plan.n) {
+      int x0 = geo_.nx, x1 = -1, z0 = nz, z1 = -1;
+      for (const auto &t : terms) {
+        x0 = std::min(x0, t.cell / nz);
+        x1 = std::max(x1, t.cell / nz);
+        z0 = std::min(z0, t.cell % nz);
+        z1 = std::max(z1, t.cell % nz);
+      }
+      plan.x0 = x0;
+      plan.z0 = z0;
+      plan.w = x1 - x0 + 1;
+      plan.h = z1 - z0 + 1;
+      std::vector<int> map(static_cast<size_t>(plan.w) * plan.h, -1);
+      for (int k = plan.n - 1; k >= 0; --k) {
+        const int cx = terms[k].cell / nz - x0, cz = terms[k].cell % nz - z0;
+        map[static_cast<size_t>(cx) * plan.h + cz] = k;
+      }
+      plan_terms_[p].allocate(terms.size() * sizeof(InjTerm));
+      plan_maps_[p].allocate(map.size() * sizeof(int));
+      cuda_check(cudaMemcpy(plan_terms_[p].get(), terms.data(), terms.size() * sizeof(InjTerm),
+                            cudaMemcpyHostToDevice),
+                 "upload injection terms");
+      cuda_check(cudaMemcpy(plan_maps_[p].get(), map.data(), map.size() * sizeof(int),
+                            cudaMemcpyHostToDevice),
+                 "upload injection map");
+      plan.terms = plan_terms_[p].as<InjTerm>();
+      plan.map = plan_maps_[p].as<int>();
+    }
+    plans_[p] = plan;
+  }
+}
+
+void Model::ensure_snapshots() {
+  if (accu_[0].get()) return;
+  const size_t n = static_cast<size_t>(cfg_.n_shots) * geo_.snapshots * grid_size();
+  for (auto &a : accu_) a.allocate(n * elem());
+}
+
+size_t Model::device_bytes() const {
+  size_t total = 0;
+  auto add = [&](const DeviceBuffer &b) { total += b.bytes(); };
+  for (auto &b : fields_) add(b);
+  for (auto &b : accu_) add(b);
+  for (auto &b : klame_) add(b);
+  for (auto &b : kvel_) add(b);
+  for (int k = 0; k < 2; ++k) {
+    add(rtf_[k]);
+    add(rtf_true_[k]);
+    add(a_stf_[k]);
+  }
+  add(lm_);
+  add(la_);
+  add(mu_);
+  add(b_);
+  add(vp_);
+  add(vs_);
+  add(rho_);
+  add(rec_raw_);
+  add(stf_d_);
+  for (auto &b : plan_terms_) add(b);
+  for (auto &b : plan_maps_) add(b);
+  return total;
+}
+
+SolverArgs Model::solver_args() {
+  SolverArgs a;
+  a.nx = geo_.nx;
+  a.nz = geo_.nz;
+  a.nt = cfg_.nt;
+  a.np = cfg_.np_boundary;
+  a.si = cfg_.snapshot_interval;
+  a.snapshots = geo_.snapshots;
+  a.nr = cfg_.nr;
+  a.dt = cfg_.dt;
+  a.dx = cfg_.dx;
+  a.dz = cfg_.dz;
+  a.vx = fields_[0].get();
+  a.vz = fields_[1].get();
+  a.txx = fields_[2].get();
+  a.tzz = fields_[3].get();
+  a.txz = fields_[4].get();
+  a.lm = lm_.get();
+  a.la = la_.get();
+  a.mu = mu_.get();
+  a.b = b_.get();
+  a.taper_tab = taper_tab_d_.get();
+  for (int k = 0; k < 5; ++k) a.accu[k] = accu_[k].get();
+  a.rec_cell = rec_cell_.as<int>();
+  a.rec_raw = rec_raw_.get();
+  a.rtf_ux = rtf_[0].as<double>();
+  a.rtf_uz = rtf_[1].as<double>();
+  a.a_stf_ux = a_stf_[0].as<double>();
+  a.a_stf_uz = a_stf_[1].as<double>();
+  a.stf = stf_d_.as<double>();
+  a.k_lam = klame_[0].as<double>();
+  a.k_mu = klame_[1].as<double>();
+  a.k_rho = klame_[2].as<double>();
+  a.fx0 = geo_.fx0;
+  a.fx1 = geo_.fx1;
+  a.fz0 = geo_.fz0;
+  a.fz1 = geo_.fz1;
+  return a;
+}
+
+void Model::synchronize() {
+  DeviceGuard guard(device_);
+  cuda_check(cudaStreamSynchronize(stream()), "cudaStreamSynchronize");
+}
+
+void Model::finish(const char *what) {
+  cuda_check(cudaGetLastError(), what);
+  if (!async_) synchronize();
+}
+
+void Model::widen(size_t n, const void *src, double *dst) {
+  cuda_check(prec_ == PSV_FP64 ? widen_f64(n, src, dst, stream()) : widen_f32(n, src, dst, stream()),
+             "widen");
+}
+
+// ----------------------------------------------------------- simulation --
+
+void Model::forward_simulate(int shot, bool store, bool verbose, bool output_wavefields,
+                             int n_steps) {
+  if (shot < 0 || shot >= cfg_.n_shots) throw Error(PSV_ERR_INVALID_ARGUMENT, "i_shot out of range");
+  if (n_steps < 0 || n_steps > cfg_.nt) n_steps = cfg_.nt;
+  DeviceGuard guard(device_);
+  if (store) ensure_snapshots();
+  SolverArgs a = solver_args();
+  const InjPlan &plan = plans_[shot];
+  auto t0 = std::chrono::steady_clock::now();
+  auto run = [&](int it0, int it1, bool zero, bool fin) {
+    cudaError_t e = prec_ == PSV_FP64
+                        ? forward_f64(a, plan, shot, store, it0, it1, zero, fin, stream())
+                        : forward_f32(a, plan, shot, store, it0, it1, zero, fin, stream());
+    cuda_check(e, "forward_simulate");
+  };
+  if (!output_wavefields) {
+    run(0, n_steps, true, true);
+  } else {
+    // Text dumps of vx, vz after every 10th step (src/fdModel.cpp:753-776).
+    for (int it0 = 0; it0 < n_steps; it0 += 10) {
+      const int it1 = std::min(n_steps, it0 + 1);
+      run(it0, it1, it0 == 0, false);
+      dump_wavefields_text(it0);
+      if (it1 < std::min(n_steps, it0 + 10)) run(it1, std::min(n_steps, it0 + 10), false, false);
+    }
+    run(n_steps, n_steps, false, true);
+  }
+  finish("forward_simulate");
+  if (verbose) {
+    synchronize();
+    double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::cout << "Seconds elapsed for forward wave simulation: " << s << std::endl;
+  }
+}
+
+int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *kernel_ms,
+                           int max_kernels) {
+  if (shot < 0 || shot >= cfg_.n_shots) throw Error(PSV_ERR_INVALID_ARGUMENT, "i_shot out of range");
+  if (n_steps <= 0 || n_steps > cfg_.nt) n_steps = cfg_.nt;
+  DeviceGuard guard(device_);
+  const int per = kKernelsPerStep + 1;
+  std::vector<cudaEvent_t> ev(static_cast<size_t>(per) * n_steps);
+  for (auto &e : ev) cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+  SolverArgs a = solver_args();
+  a.events = ev.data();
+  cudaError_t err =
+      prec_ == PSV_FP64
+          ? forward_f64(a, plans_[shot], shot, false, 0, n_steps, true, false, stream())
+          : forward_f32(a, plans_[shot], shot, false, 0, n_steps, true, false, stream());
+  cudaError_t sync = cudaStreamSynchronize(stream());
+  std::vector<double> sums(kKernelsPerStep, 0.0);
+  double total = 0;
+  if (err == cudaSuccess && sync == cudaSuccess) {
+    for (int s = 0; s < n_steps; ++s) {
+      for (int k = 0; k < kKernelsPerStep; ++k) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev[per * s + k], ev[per * s + k + 1]);
+        sums[k] += ms;
+      }
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev.front(), ev.back());
+    total = ms;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  cuda_check(err, "profile_forward");
+  cuda_check(sync, "profile_forward");
+  if (per_step_ms) *per_step_ms = total / n_steps;
+  for (int k = 0; k < kKernelsPerStep && k < max_kernels; ++k)
+    if (kernel_ms) kernel_ms[k] = sums[k] / n_steps;
+  return kKernelsPerStep;
+}
+
+void Model::adjoint_simulate(int shot, bool verbose) {
+  if (shot < 0 || shot >= cfg_.n_shots) throw Error(PSV_ERR_INVALID_ARGUMENT, "i_shot out of range");
+  DeviceGuard guard(device_);
+  ensure_snapshots();
+  SolverArgs a = solver_args();
+  auto t0 = std::chrono::steady_clock::now();
+  cudaError_t e = prec_ == PSV_FP64 ? adjoint_f64(a, plans_[cfg_.n_shots], shot, stream())
+                                    : adjoint_f32(a, plans_[cfg_.n_shots], shot, stream());
+  cuda_check(e, "adjoint_simulate");
+  finish("adjoint_simulate");
+  if (verbose) {
+    synchronize();
+    double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::cout << "Seconds elapsed for adjoint wave simulation: " << s << std::endl;
+  }
+}
+
+double Model::calculate_l2_misfit() {
+  DeviceGuard guard(device_);
+  const size_t n = data_size();
+  int parts = static_cast<int>(std::min<size_t>(kPartials, (n + 255) / 256));
+  if (parts < 1) parts = 1;
+  cuda_check(misfit_l2(n, cfg_.dt, rtf_true_[0].as<double>(), rtf_[0].as<double>(),
+                       rtf_true_[1].as<double>(), rtf_[1].as<double>(), partials_.as<double>(),
+                       parts, scalar_.as<double>(), stream()),
+             "calculate_l2_misfit");
+  double out = 0;
+  cuda_check(cudaMemcpyAsync(&out, scalar_.get(), sizeof(double), cudaMemcpyDeviceToHost, stream()),
+             "misfit copy");
+  synchronize();
+  misfit_ = out;
+  return out;
+}
+
+void Model::calculate_l2_adjoint_sources() {
+  DeviceGuard guard(device_);
+  cuda_check(adjoint_sources_l2(data_size(), rtf_[0].as<double>(), rtf_true_[0].as<double>(),
+                                rtf_[1].as<double>(), rtf_true_[1].as<double>(),
+                                a_stf_[0].as<double>(), a_stf_[1].as<double>(), stream()),
+             "calculate_l2_adjoint_sources");
+  finish("calculate_l2_adjoint_sources");
+}
+
+void Model::reset_kernels() {
+  DeviceGuard guard(device_);
+  for (auto &k : klame_)
+    cuda_check(cudaMemsetAsync(k.get(), 0, k.bytes(), stream()), "reset_kernels");
+  finish("reset_kernels");
+}
+
+void Model::map_kernels_to_velocity() {
+  DeviceGuard guard(device_);
+  cuda_check(map_kernels(grid_size(), vp_.as<double>(), vs_.as<double>(), rho_.as<double>(),
+                         klame_[0].as<double>(), klame_[1].as<double>(), klame_[2].as<double>(),
+                         kvel_[0].as<double>(), kvel_[1].as<double>(), kvel_[2].as<double>(),
+                         stream()),
+             "map_kernels_to_velocity");
+  finish("map_kernels_to_velocity");
+}
+
+void Model::run_model(bool verbose, bool simulate_adjoint) {
+  const bool was_async = async_;
+  async_ = true;
+  try {
+    for (int s = 0; s < cfg_.n_shots; ++s) forward_simulate(s, true, verbose, false);
+    calculate_l2_misfit();
+    if (simulate_adjoint) {
+      calculate_l2_adjoint_sources();
+      reset_kernels();
+      for (int s = 0; s < cfg_.n_shots; ++s) adjoint_simulate(s, verbose);
+      map_kernels_to_velocity();
+    }
+  } catch (...) {
+    async_ = was_async;
+    throw;
+  }
+  async_ = was_async;
+  finish("run_model");
+}
+
+void Model::update_from_velocity() {
+  DeviceGuard guard(device_);
+  const int n = static_cast<int>(grid_size());
+  cudaError_t e =
+      prec_ == PSV_FP64
+          ? medium_f64(n, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(), lm_.get(),
+                       la_.get(), mu_.get(), b_.get(), stream())
+          : medium_f32(n, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(), lm_.get(),
+                       la_.get(), mu_.get(), b_.get(), stream());
+  cuda_check(e, "update_from_velocity");
+  finish("update_from_velocity");
+}
+
+// ------------------------------------------------------------ transfers --
+
+void Model::get_parameter_fields(double *vp, double *vs, double *rho) {
+  DeviceGuard guard(device_);
+  const size_t bytes = grid_size() * sizeof(double);
+  double *out[3] = {vp, vs, rho};
+  DeviceBuffer *src[3] = {&vp_, &vs_, &rho_};
+  for (int k = 0; k < 3; ++k)
+    if (out[k])
+      cuda_check(cudaMemcpyAsync(out[k], src[k]->get(), bytes, cudaMemcpyDeviceToHost, stream()),
+                 "get_parameter_fields");
+  synchronize();
+}
+
+void Model::set_parameter_fields(const double *vp, const double *vs, const double *rho,
+                                 bool device_pointers) {
+  DeviceGuard guard(device_);
+  const size_t bytes = grid_size() * sizeof(double);
+  const double *in[3] = {vp, vs, rho};
+  DeviceBuffer *dst[3] = {&vp_, &vs_, &rho_};
+  for (int k = 0; k < 3; ++k)
+    cuda_check(cudaMemcpyAsync(dst[k]->get(), in[k], bytes,
+                               device_pointers ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               stream()),
+               "set_parameter_fields");
+  update_from_velocity();
+}
+
+void Model::load_model(const std::string &de_path, const std::string &vp_path,
+                       const std::string &vs_path, bool verbose) {
+  std::ifstream de(de_path), vp(vp_path), vs(vs_path);
+  if (verbose) {
+    std::cout << "Loading models." << std::endl;
+    std::cout << "File: " << de_path << std::endl
+              << "File for density is " << (de.good() ? "good (exists at least)." : "ungood.")
+              << std::endl;
+    std::cout << "File: " << vp_path << std::endl
+              << "File for P-wave velocity is "
+              << (vp.good() ? "good (exists at least)." : "ungood.") << std::endl;
+    std::cout << "File: " << vs_path << std::endl
+              << "File for S-wave velocity is "
+              << (vs.good() ? "good (exists at least)." : "ungood.") << std::endl;
+  }
+  if (!de.good() || !vp.good() || !vs.good())
+    throw Error(PSV_ERR_IO, "The files for target models don't seem to exist.\r\nPaths:\r\n"
+                            "\tDensity target: " + de_path + "\r\n\tP-wave target : " + vp_path +
+                                "\r\n\tS-wave target : " + vs_path + "\r\n");
+  const size_t n = grid_size();
+  std::vector<double> r(n), p(n), s(n);
+  for (size_t i = 0; i < n; ++i) {
+    de >> r[i];
+    vp >> p[i];
+    vs >> s[i];
+    if (!de.good() || !vp.good() || !vs.good())
+      throw Error(PSV_ERR_IO,
+                  "Received bad state of one of the files at end of reading. Does the data match "
+                  "the domain?");
+  }
+  double extra;
+  de >> extra;
+  vp >> extra;
+  vs >> extra;
+  if (de.good() || vp.good() || vs.good()) throw Error(PSV_ERR_IO, "Too much data is present!");
+  set_parameter_fields(p.data(), s.data(), r.data(), false);
+  synchronize();
+}
+
+void Model::get_kernels(double *vp_k, double *vs_k, double *rho_k, bool device_pointers) {
+  DeviceGuard guard(device_);
+  const size_t bytes = grid_size() * sizeof(double);
+  double *out[3] = {vp_k, vs_k, rho_k};
+  for (int k = 0; k < 3; ++k)
+    if (out[k])
+      cuda_check(cudaMemcpyAsync(out[k], kvel_[k].get(), bytes,
+                                 device_pointers ? cudaMemcpyDeviceToDevice
+                                                 : cudaMemcpyDeviceToHost,
+                                 stream()),
+                 "get_kernels");
+  if (!device_pointers) synchronize();
+}
+
+void Model::get_lame_kernels(double *lam, double *mu, double *rho) {
+  DeviceGuard guard(device_);
+  const size_t bytes = grid_size() * sizeof(double);
+  double *out[3] = {lam, mu, rho};
+  for (int k = 0; k < 3; ++k)
+    if (out[k])
+      cuda_check(cudaMemcpyAsync(out[k], klame_[k].get(), bytes, cudaMemcpyDeviceToHost, stream()),
+                 "get_lame_kernels");
+  synchronize();
+}
+
+void Model::get_data(int which, double *ux, double *uz, bool device_pointers) {
+  DeviceGuard guard(device_);
+  DeviceBuffer *src = which == kSynthetic ? rtf_ : which == kObserved ? rtf_true_ : a_stf_;
+  const size_t bytes = data_size() * sizeof(double);
+  double *out[2] = {ux, uz};
+  for (int k = 0; k < 2; ++k)
+    if (out[k] && bytes)
+      cuda_check(cudaMemcpyAsync(out[k], src[k].get(), bytes,
+                                 device_pointers ? cudaMemcpyDeviceToDevice
+                                                 : cudaMemcpyDeviceToHost,
+                                 stream()),
+                 "get data");
+  if (!device_pointers) synchronize();
+}
+
+void Model::set_data(int which, const double *ux, const double *uz, bool device_pointers) {
+  DeviceGuard guard(device_);
+  DeviceBuffer *dst = which == kSynthetic ? rtf_ : which == kObserved ? rtf_true_ : a_stf_;
+  const size_t bytes = data_size() * sizeof(double);
+  const double *in[2] = {ux, uz};
+  for (int k = 0; k < 2; ++k)
+    if (bytes)
+      cuda_check(cudaMemcpyAsync(dst[k].get(), in[k], bytes,
+                                 device_pointers ? cudaMemcpyDeviceToDevice
+                                                 : cudaMemcpyHostToDevice,
+                                 stream()),
+                 "set data");
+  finish("set data");
+}
+
+void Model::get_snapshots(double *out[5]) {
+  DeviceGuard guard(device_);
+  ensure_snapshots();
+  const size_t n = static_cast<size_t>(cfg_.n_shots) * geo_.snapshots * grid_size();
+  const size_t chunk = std::min<size_t>(n, size_t(1) << 24);
+  DeviceBuffer tmp;
+  if (prec_ != PSV_FP64) tmp.allocate(chunk * sizeof(double));
+  for (int f = 0; f < 5; ++f) {
+    if (!out[f]) continue;
+    for (size_t off = 0; off < n; off += chunk) {
+      const size_t m = std::min(chunk, n - off);
+      if (prec_ == PSV_FP64) {
+        cuda_check(cudaMemcpyAsync(out[f] + off, accu_[f].as<double>() + off, m * sizeof(double),
+                                   cudaMemcpyDeviceToHost, stream()),
+                   "get_snapshots");
+      } else {
+        widen(m, accu_[f].as<float>() + off, tmp.as<double>());
+        cuda_check(cudaMemcpyAsync(out[f] + off, tmp.get(), m * sizeof(double),
+                                   cudaMemcpyDeviceToHost, stream()),
+                   "get_snapshots");
+      }
+      synchronize();
+    }
+  }
+}
+
+void Model::get_wavefields(double *out[5]) {
+  DeviceGuard guard(device_);
+  const size_t n = grid_size();
+  DeviceBuffer tmp;
+  if (prec_ != PSV_FP64) tmp.allocate(n * sizeof(double));
+  for (int f = 0; f < 5; ++f) {
+    if (!out[f]) continue;
+    if (prec_ == PSV_FP64) {
+      cuda_check(cudaMemcpyAsync(out[f], fields_[f].get(), n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, stream()),
+                 "get_wavefields");
+    } else {
+      widen(n, fields_[f].get(), tmp.as<double>());
+      cuda_check(cudaMemcpyAsync(out[f], tmp.get(), n * sizeof(double), cudaMemcpyDeviceToHost,
+                                 stream()),
+                 "get_wavefields");
+    }
+    synchronize();
+  }
+}
+
+void Model::get_stf(double *out) const { std::copy(stf_.begin(), stf_.end(), out); }
+void Model::get_moment(double *out) const { std::copy(moment_.begin(), moment_.end(), out); }
+
+void Model::get_taper(double *out) const {
+  const int nx = geo_.nx, nz = geo_.nz, np = cfg_.np_boundary;
+  for (int ix = 0; ix < nx; ++ix)
+    for (int iz = 0; iz < nz; ++iz) {
+      int c = std::min(std::min(ix + 1, iz + 1), std::min(nx - ix, nz - iz));
+      c = std::min(c, np);
+      out[static_cast<size_t>(ix) * nz + iz] = taper_tab_[c];
+    }
+}
+
+// ------------------------------------------------------ model vectors ---
+
+void Model::get_model_vector(double *out) {
+  std::vector<double> vp(grid_size()), vs(grid_size()), rho(grid_size());
+  get_parameter_fields(vp.data(), vs.data(), rho.data());
+  const int npx = cfg_.npx, npz = cfg_.npz, nz = geo_.nz;
+  const int bx = geo_.nx_free / npx, bz = geo_.nz_free / npz, per = bx * bz;
+  for (int ix = 0; ix < bx; ++ix)
+    for (int iz = 0; iz < bz; ++iz) {
+      const int p = ix + iz * geo_.nx_free / npx;
+      const int gx = ix * npx + cfg_.nx_inner_boundary + cfg_.np_boundary;
+      const int gz = iz * npz + cfg_.nz_inner_boundary + cfg_.np_boundary;
+      out[p] = out[p + per] = out[p + 2 * per] = 0;
+      for (int sx = 0; sx < npx; ++sx)
+        for (int sz = 0; sz < npz; ++sz) {
+          const size_t i = static_cast<size_t>(gx + sx) * nz + gz + sz;
+          out[p] += vp[i] / (npx * npz);
+          out[p + per] += vs[i] / (npx * npz);
+          out[p + 2 * per] += rho[i] / (npx * npz);
+        }
+    }
+}
+
+void Model::set_model_vector(const double *in) {
+  std::vector<double> vp(grid_size()), vs(grid_size()), rho(grid_size());
+  get_parameter_fields(vp.data(), vs.data(), rho.data());
+  const int npx = cfg_.npx, npz = cfg_.npz, nz = geo_.nz;
+  const int bx = geo_.nx_free / npx, bz = geo_.nz_free / npz, per = bx * bz;
+  for (int ix = 0; ix < bx; ++ix)
+    for (int iz = 0; iz < bz; ++iz) {
+      const int p = ix + iz * geo_.nx_free / npx;
+      const int gx = ix * npx + cfg_.nx_inner_boundary + cfg_.np_boundary;
+      const int gz = iz * npz + cfg_.nz_inner_boundary + cfg_.np_boundary;
+      for (int sx = 0; sx < npx; ++sx)
+        for (int sz = 0; sz < npz; ++sz) {
+          const size_t i = static_cast<size_t>(gx + sx) * nz + gz + sz;
+          vp[i] = in[p];
+          vs[i] = in[p + per];
+          rho[i] = in[p + 2 * per];
+        }
+    }
+  set_parameter_fields(vp.data(), vs.data(), rho.data(), false);
+  synchronize();
+}
+
+void Model::get_gradient_vector(double *out) {
+  std::vector<double> kp(grid_size()), ks(grid_size()), kr(grid_size());
+  get_kernels(kp.data(), ks.data(), kr.data(), false);
+  const int npx = cfg_.npx, npz = cfg_.npz, nz = geo_.nz;
+  const int bx = geo_.nx_free / npx, bz = geo_.nz_free / npz, per = bx * bz;
+  for (int ix = 0; ix < bx; ++ix)
+    for (int iz = 0; iz < bz; ++iz) {
+      const int p = ix + iz * geo_.nx_free / npx;
+      const int gx = ix * npx + cfg_.nx_inner_boundary + cfg_.np_boundary;
+      const int gz = iz * npz + cfg_.nz_inner_boundary + cfg_.np_boundary;
+      out[p] = out[p + per] = out[p + 2 * per] = 0;
+      for (int sx = 0; sx < npx; ++sx)
+        for (int sz = 0; sz < npz; ++sz) {
+          const size_t i = static_cast<size_t>(gx + sx) * nz + gz + sz;
+          out[p] += kp[i];
+          out[p + per] += ks[i];
+          out[p + 2 * per] += kr[i];
+        }
+    }
+}
+
+void Model::load_vector(const std::string &path, bool verbose, double *out) const {
+  const int n = 3 * geo_.nx_free * geo_.nz_free;
+  std::ifstream f(path);
+  if (verbose)
+    std::cout << "Loading model vector." << std::endl
+              << "File: " << path << std::endl
+              << "File is " << (f.good() ? "good (exists at least)." : "ungood.") << std::endl;
+  if (!f.good())
+    throw Error(PSV_ERR_IO, "The files for target models don't seem to exist.\r\nPaths:\r\n"
+                            "\tDensity target: " + path + "\r\n");
+  for (int i = 0; i < n; ++i) f >> out[i];
+  if (!f.good()) throw Error(PSV_ERR_IO, "Not enough data is present!");
+  double extra;
+  f >> extra;
+  if (f.good()) throw Error(PSV_ERR_IO, "Too much data is present!");
+}
+
+// ------------------------------------------------------------ geometry --
+
+void Model::get_sources(bool in_units, bool include_boundary, double *x, double *z) const {
+  for (int i = 0; i < cfg_.n_sources; ++i) {
+    x[i] = ix_src_[i];
+    z[i] = iz_src_[i];
+    if (!include_boundary || in_units) {
+      x[i] -= cfg_.np_boundary;
+      z[i] -= cfg_.np_boundary;
+      if (in_units) {
+        x[i] *= cfg_.dx;
+        z[i] *= cfg_.dz;
+      }
+    }
+  }
+}
+
+void Model::get_receivers(bool in_units, bool include_boundary, double *x, double *z) const {
+  for (int i = 0; i < cfg_.nr; ++i) {
+    x[i] = ix_rec_[i];
+    z[i] = iz_rec_[i];
+    if (!include_boundary || in_units) {
+      x[i] -= cfg_.np_boundary;
+      z[i] -= cfg_.np_boundary;
+      if (in_units) {
+        x[i] *= cfg_.dx;
+        z[i] *= cfg_.dz;
+      }
+    }
+  }
+}
+
+void Model::get_coordinates(bool in_units, double *ix_out, double *iz_out) const {
+  const int nx = geo_.nx, nz = geo_.nz, np = cfg_.np_boundary;
+  for (int ix = 0; ix < nx; ++ix)
+    for (int iz = 0; iz < nz; ++iz) {
+      const size_t i = static_cast<size_t>(ix) * nz + iz;
+      if (in_units) {
+        ix_out[i] = (ix - np) * cfg_.dx;
+        iz_out[i] = (iz - np) * cfg_.dz;
+      } else {
+        ix_out[i] = ix;
+        iz_out[i] = iz;
+      }
+    }
+}
+
+void Model::get_extent(bool include_boundary, double *o) const {
+  if (include_boundary) {
+    o[0] = -cfg_.np_boundary;
+    o[1] = cfg_.dx * (cfg_.nx_inner + cfg_.np_boundary);
+    o[2] = -cfg_.np_boundary;
+    o[3] = cfg_.dz * (cfg_.nz_inner + cfg_.np_boundary);
+  } else {
+    o[0] = 0;
+    o[1] = cfg_.dx * cfg_.nx_inner;
+    o[2] = 0;
+    o[3] = cfg_.dz * cfg_.nz_inner;
+  }
+}
+
+// ------------------------------------------------------------ text I/O --
+
+void Model::write_receivers(const std::string &) {
+  // The reference accepts a prefix but writes to the same names regardless
+  // (src/fdModel.cpp:973-1006).
+  std::vector<double> ux(data_size()), uz(data_size());
+  get_data(kSynthetic, ux.data(), uz.data(), false);
+  const int nr = cfg_.nr, nt = cfg_.nt;
+  for (int s = 0; s < cfg_.n_shots; ++s) {
+    std::ofstream fx(cfg_.observed_data_folder + "/rtf_ux" + std::to_string(s) + ".txt");
+    std::ofstream fz(cfg_.observed_data_folder + "/rtf_uz" + std::to_string(s) + ".txt");
+    if (!fx.good() || !fz.good()) throw Error(PSV_ERR_IO, "cannot write receiver files");
+    fx.precision(std::numeric_limits<double>::digits10 + 10);
+    fz.precision(std::numeric_limits<double>::digits10 + 10);
+    for (int r = 0; r < nr; ++r) {
+      fx << std::endl;
+      fz << std::endl;
+      for (int it = 0; it < nt; ++it) {
+        const size_t i = (static_cast<size_t>(s) * nr + r) * nt + it;
+        fx << ux[i] << " ";
+        fz << uz[i] << " ";
+      }
+    }
+  }
+}
+
+void Model::load_receivers(bool verbose) {
+  const int nr = cfg_.nr, nt = cfg_.nt;
+  std::vector<double> ux(data_size()), uz(data_size());
+  for (int s = 0; s < cfg_.n_shots; ++s) {
+    std::ifstream fx(cfg_.observed_data_folder + "/rtf_ux" + std::to_string(s) + ".txt");
+    std::ifstream fz(cfg_.observed_data_folder + "/rtf_uz" + std::to_string(s) + ".txt");
+    if (verbose) {
+      std::cout << "File for ux data at shot " << s << " is "
+                << (fx.good() ? "good (exists at least)." : "ungood.") << std::endl;
+      std::cout << "File for uz data at shot " << s << " is "
+                << (fz.good() ? "good (exists at least)." : "ungood.") << std::endl;
+    }
+    if (!fx.good() || !fz.good()) throw Error(PSV_ERR_IO, "Not all data is present!");
+    for (int r = 0; r < nr; ++r)
+      for (int it = 0; it < nt; ++it) {
+        const size_t i = (static_cast<size_t>(s) * nr + r) * nt + it;
+        fx >> ux[i];
+        fz >> uz[i];
+      }
+    if (!fx.good() || !fz.good()) throw Error(PSV_ERR_IO, "Not enough data is present!");
+    double extra;
+    fx >> extra;
+    fz >> extra;
+    if (fx.good() || fz.good()) throw Error(PSV_ERR_IO, "Too much data is present!");
+  }
+  set_data(kObserved, ux.data(), uz.data(), false);
+  synchronize();
+}
+
+void Model::write_sources() const {
+  const int nt = cfg_.nt;
+  for (int s = 0; s < cfg_.n_shots; ++s) {
+    std::ofstream f(cfg_.stf_folder + "/sources_shot_" + std::to_string(s) + ".txt");
+    if (!f.good()) throw Error(PSV_ERR_IO, "cannot write source files");
+    f.precision(std::numeric_limits<double>::digits10 + 10);
+    for (int src : cfg_.shots[s]) {
+      f << std::endl;
+      for (int it = 0; it < nt; ++it) f << stf_[static_cast<size_t>(src) * nt + it] << " ";
+    }
+  }
+}
+
+void Model::write_kernels() {
+  const size_t n = grid_size();
+  std::vector<double> kp(n), ks(n), kr(n);
+  get_kernels(kp.data(), ks.data(), kr.data(), false);
+  std::ofstream fp("kernel_vp.txt"), fs("kernel_vs.txt"), fr("kernel_density.txt");
+  if (!fp.good() || !fs.good() || !fr.good()) throw Error(PSV_ERR_IO, "cannot write kernel files");
+  for (int ix = 0; ix < geo_.nx; ++ix) {
+    for (int iz = 0; iz < geo_.nz; ++iz) {
+      const size_t i = static_cast<size_t>(ix) * geo_.nz + iz;
+      fp << kp[i] << " ";
+      fs << ks[i] << " ";
+      fr << kr[i] << " ";
+    }
+    fp << std::endl;
+    fs << std::endl;
+    fr << std::endl;
+  }
+}
+
+void Model::dump_wavefields_text(int it) {
+  std::vector<double> vx(grid_size()), vz(grid_size());
+  double *out[5] = {vx.data(), vz.data(), nullptr, nullptr, nullptr};
+  get_wavefields(out);
+  std::ofstream fx("snapshots/vx" + pad5(it) + ".txt"), fz("snapshots/vz" + pad5(it) + ".txt");
+  for (int ix = 0; ix < geo_.nx; ++ix) {
+    for (int iz = 0; iz < geo_.nz; ++iz) {
+      const size_t i = static_cast<size_t>(ix) * geo_.nz + iz;
+      fx << vx[i] << " ";
+      fz << vz[i] << " ";
+    }
+    fx << std::endl;
+    fz << std::endl;
+  }
+}
+
+}  // namespace psv

@@ -1,0 +1,168 @@
+// One P-SV model resident on a GPU: the GB300 counterpart of the reference's
+// fdModel class (src/fdModel.h:35-318). The configuration and setup tables
+// live on the host; every array the time loop touches lives in device memory.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "psv_config.hpp"
+#include "psv_solver.hpp"
+
+namespace psv {
+
+// Owning device allocation.
+class DeviceBuffer {
+ public:
+  DeviceBuffer() = default;
+  ~DeviceBuffer();
+  DeviceBuffer(const DeviceBuffer &) = delete;
+  DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+  DeviceBuffer(DeviceBuffer &&o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_) {
+    o.ptr_ = nullptr;
+    o.bytes_ = 0;
+  }
+  DeviceBuffer &operator=(DeviceBuffer &&o) noexcept {
+    if (this != &o) {
+      release();
+      ptr_ = o.ptr_;
+      bytes_ = o.bytes_;
+      o.ptr_ = nullptr;
+      o.bytes_ = 0;
+    }
+    return *this;
+  }
+  void allocate(size_t bytes);  // zero-filled
+  void release();
+  void *get() const { return ptr_; }
+  size_t bytes() const { return bytes_; }
+  template <typename U>
+  U *as() const {
+    return static_cast<U *>(ptr_);
+  }
+
+ private:
+  void *ptr_ = nullptr;
+  size_t bytes_ = 0;
+};
+
+// Throws Error(PSV_ERR_CUDA) when e is not cudaSuccess.
+void cuda_check(cudaError_t e, const char *what);
+
+class Model {
+ public:
+  Model(const Config &cfg, int precision, int device);
+  Model(const Model &other);  // deep copy (src/fdModel.cpp:64-97)
+  ~Model();
+
+  const Config &config() const { return cfg_; }
+  const Geometry &geometry() const { return geo_; }
+  int precision() const { return prec_; }
+  int device() const { return device_; }
+  double misfit() const { return misfit_; }
+  size_t device_bytes() const;
+
+  // Simulation (src/fdModel.cpp:526-969, 1128-1183, 1291-1324).
+  void forward_simulate(int shot, bool store, bool verbose, bool output_wavefields,
+                        int n_steps = -1);
+  void adjoint_simulate(int shot, bool verbose);
+  double calculate_l2_misfit();
+  void calculate_l2_adjoint_sources();
+  void reset_kernels();
+  void map_kernels_to_velocity();
+  void run_model(bool verbose, bool simulate_adjoint);
+  void update_from_velocity();
+  // Forward time steps of `shot` with CUDA events around every launch;
+  // fills the average device time per step and per launch kind (ms).
+  int profile_forward(int shot, int n_steps, double *per_step_ms, double *kernel_ms,
+                      int max_kernels);
+
+  // Transfers of host FP64 arrays.
+  void get_parameter_fields(double *vp, double *vs, double *rho);
+  void set_parameter_fields(const double *vp, const double *vs, const double *rho,
+                            bool device_pointers);
+  void load_model(const std::string &de, const std::string &vp, const std::string &vs,
+                  bool verbose);
+  void get_kernels(double *vp_k, double *vs_k, double *rho_k, bool device_pointers);
+  void get_lame_kernels(double *lam, double *mu, double *rho);
+  void get_data(int which, double *ux, double *uz, bool device_pointers);
+  void set_data(int which, const double *ux, const double *uz, bool device_pointers);
+  void get_snapshots(double *out[5]);
+  void get_wavefields(double *out[5]);
+  void get_stf(double *out) const;
+  void get_moment(double *out) const;
+  void get_taper(double *out) const;
+
+  void get_model_vector(double *out);
+  void set_model_vector(const double *in);
+  void get_gradient_vector(double *out);
+  void load_vector(const std::string &path, bool verbose, double *out) const;
+
+  void get_sources(bool in_units, bool include_boundary, double *x, double *z) const;
+  void get_receivers(bool in_units, bool include_boundary, double *x, double *z) const;
+  void get_coordinates(bool in_units, double *ix, double *iz) const;
+  void get_extent(bool include_boundary, double *out4) const;
+
+  void write_receivers(const std::string &prefix);
+  void load_receivers(bool verbose);
+  void write_sources() const;
+  void write_kernels();
+
+  void set_stream(cudaStream_t s) { user_stream_ = s; }
+  cudaStream_t stream() const { return user_stream_ ? user_stream_ : stream_; }
+  void set_async(bool a) { async_ = a; }
+  void synchronize();
+
+  enum DataKind { kSynthetic = 0, kObserved = 1, kAdjoint = 2 };
+
+ private:
+  void allocate();
+  void build_tables();
+  void build_plans();
+  void ensure_snapshots();
+  SolverArgs solver_args();
+  void finish(const char *what);
+  size_t grid_size() const { return static_cast<size_t>(geo_.nx) * geo_.nz; }
+  size_t data_size() const { return static_cast<size_t>(cfg_.n_shots) * cfg_.nr * cfg_.nt; }
+  size_t elem() const { return prec_ == 1 ? sizeof(double) : sizeof(float); }
+  void widen(size_t n, const void *src, double *dst_device);
+  void dump_wavefields_text(int it);
+
+  Config cfg_;
+  Geometry geo_;
+  int prec_;
+  int device_;
+  cudaStream_t stream_ = nullptr;
+  cudaStream_t user_stream_ = nullptr;
+  bool async_ = false;
+  double misfit_ = 0;
+
+  // Host setup tables (src/fdModel.cpp:193-299).
+  std::vector<int> ix_src_, iz_src_, ix_rec_, iz_rec_;  // absolute indices
+  std::vector<double> stf_;                             // [n_sources][nt]
+  std::vector<double> moment_;                          // [n_sources][2][2]
+  std::vector<double> taper_tab_;                       // [np + 1]
+
+  // Device arrays.
+  DeviceBuffer fields_[5];                    // vx vz txx tzz txz   (T)
+  DeviceBuffer lm_, la_, mu_, b_;             // medium              (T)
+  DeviceBuffer vp_, vs_, rho_;                // medium              (FP64)
+  DeviceBuffer taper_tab_d_;                  // (T)
+  DeviceBuffer accu_[5];                      // snapshots           (T)
+  DeviceBuffer rtf_[2], rtf_true_[2], a_stf_[2];  // data          (FP64)
+  DeviceBuffer rec_raw_;                      // [2][nr][nt]         (T)
+  DeviceBuffer rec_cell_;                     // [nr] int
+  DeviceBuffer stf_d_;                        // [n_sources][nt]     (FP64)
+  DeviceBuffer klame_[3];                     // lambda mu rho       (FP64)
+  DeviceBuffer kvel_[3];                      // vp vs rho           (FP64)
+  DeviceBuffer partials_, scalar_;            // reduction scratch   (FP64)
+  // Injection plans: one per shot (sources) and one for the adjoint receivers.
+  std::vector<DeviceBuffer> plan_terms_, plan_maps_;
+  std::vector<InjPlan> plans_;  // [n_shots] forward, [n_shots] = adjoint
+  static constexpr int kPartials = 1024;
+};
+
+}  // namespace psv

@@ -1,0 +1,101 @@
+// Host-side interface of the P-SV time-stepping kernels. The kernels are
+// templated on the wave-field precision and compiled twice:
+// psv_solver_f64.cu (double, no contraction into fused multiply-add, so the
+// arithmetic is bit-identical to the reference's src/fdModel.cpp) and
+// psv_solver_f32.cu (float, the production path).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace psv {
+
+// One additive term applied to a velocity point right after that point's
+// velocity update (source injection src/fdModel.cpp:681-751, adjoint-source
+// injection src/fdModel.cpp:951-958). Terms are kept in the reference's
+// serial order; terms of one point are contiguous.
+//   kind 0 (moment-tensor source):  v += (((coef * stf[index][it]) * dt) * b) / div
+//   kind 1 (adjoint source):        v += ((dt * b) * a_stf[field][shot][index][it]) / div
+// with coef carrying the sign of the reference's '+=' / '-='.
+struct InjTerm {
+  int cell;   // absolute grid index ix * nz + iz
+  int field;  // 0: vx, 1: vz
+  int index;  // source id (kind 0) or receiver id (kind 1)
+  int kind;
+  double coef;
+  double div;
+};
+
+// Injection terms of one shot (or of the adjoint receivers), with a dense
+// lookup table over their bounding box: map[(ix - x0) * h + (iz - z0)] is
+// the first term of that point or -1.
+struct InjPlan {
+  int x0 = 0, z0 = 0, w = 0, h = 0;
+  const int *map = nullptr;
+  const InjTerm *terms = nullptr;
+  int n = 0;
+};
+
+// Everything one forward or adjoint simulation of a shot touches. Pointers
+// typed void are arrays of the wave-field precision T; double pointers are
+// FP64 whatever T is.
+struct SolverArgs {
+  int nx = 0, nz = 0, nt = 0, np = 0, si = 1, snapshots = 0, nr = 0;
+  double dt = 0, dx = 0, dz = 0;
+  // wave fields [nx][nz]
+  void *vx = nullptr, *vz = nullptr, *txx = nullptr, *tzz = nullptr, *txz = nullptr;
+  // medium: lm = lambda + 2 mu, la = lambda, mu, b = 1 / rho  [nx][nz]
+  const void *lm = nullptr, *la = nullptr, *mu = nullptr, *b = nullptr;
+  // Cerjan taper by frame count, taper_tab[0..np] (src/fdModel.cpp:263-298)
+  const void *taper_tab = nullptr;
+  // stored forward snapshots, one array per field, [shots][snapshots][nx][nz]
+  void *accu[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // receivers: absolute cell, raw per-step velocities [2][nr][nt] (T)
+  const int *rec_cell = nullptr;
+  void *rec_raw = nullptr;
+  // seismograms, FP64 [shots][nr][nt]
+  double *rtf_ux = nullptr, *rtf_uz = nullptr;
+  const double *a_stf_ux = nullptr, *a_stf_uz = nullptr;
+  // source time functions, FP64 [n_sources][nt]
+  const double *stf = nullptr;
+  // Lame-basis kernels, FP64 [nx][nz]
+  double *k_lam = nullptr, *k_mu = nullptr, *k_rho = nullptr;
+  // free region, absolute indices [fx0, fx1) x [fz0, fz1)
+  int fx0 = 0, fx1 = 0, fz0 = 0, fz1 = 0;
+  // optional profiling: kKernelsPerStep + 1 events per forward time step,
+  // recorded before each launch of the step and after the last one
+  cudaEvent_t *events = nullptr;
+};
+
+// Launches per forward time step, in launch order, and their names.
+constexpr int kKernelsPerStep = 2;
+inline const char *step_kernel_name(int k) { return k == 0 ? "stress_step" : "velocity_step"; }
+
+// Precision-specific entry points (defined in psv_solver_f32.cu / _f64.cu).
+#define PSV_SOLVER_DECLS(SUFFIX)                                                          \
+  cudaError_t forward_##SUFFIX(const SolverArgs &a, const InjPlan &plan, int shot,       \
+                               bool store, int it0, int it1, bool zero_first,            \
+                               bool finish, cudaStream_t s);                              \
+  cudaError_t adjoint_##SUFFIX(const SolverArgs &a, const InjPlan &plan, int shot,       \
+                               cudaStream_t s);                                           \
+  cudaError_t medium_##SUFFIX(int n, const double *vp, const double *vs, const double *rho, \
+                              void *lm, void *la, void *mu, void *b, cudaStream_t s);     \
+  cudaError_t widen_##SUFFIX(size_t n, const void *src, double *dst, cudaStream_t s);    \
+  cudaError_t narrow_##SUFFIX(size_t n, const double *src, void *dst, cudaStream_t s);
+PSV_SOLVER_DECLS(f32)
+PSV_SOLVER_DECLS(f64)
+#undef PSV_SOLVER_DECLS
+
+// FP64 helpers (psv_aux.cu).
+cudaError_t misfit_l2(size_t n, double dt, const double *obs_ux, const double *syn_ux,
+                      const double *obs_uz, const double *syn_uz, double *partials,
+                      int n_partials, double *out, cudaStream_t s);
+cudaError_t adjoint_sources_l2(size_t n, const double *syn_ux, const double *obs_ux,
+                               const double *syn_uz, const double *obs_uz, double *a_ux,
+                               double *a_uz, cudaStream_t s);
+cudaError_t map_kernels(size_t n, const double *vp, const double *vs, const double *rho,
+                        const double *k_lam, const double *k_mu, const double *k_rho,
+                        double *vp_k, double *vs_k, double *rho_k, cudaStream_t s);
+
+}  // namespace psv

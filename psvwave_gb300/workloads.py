@@ -1,0 +1,86 @@
+"""Seeded synthetic workloads with the shapes of the benchmark
+configurations: model parameters (fdModel.from_parameters keywords) and
+media (vp, vs, rho on the padded [nx][nz] grid).
+
+* c0 -- 200 x 100 inner cells, 25-cell Cerjan boundary (factor 0.015),
+  dx = dz = 1.249, dt = 2.5e-4, nt = 4000; homogeneous 2000/800/1500 with a
+  radius-15-cell inclusion of +10 % vp, vs, rho at a seeded position; two
+  reverse-fault sources (dips 45 and 60 degrees) in one shot, Ricker 50 Hz,
+  delay_cycles_per_shot 24; 19 receivers along z = 10; snapshot interval 10.
+* c1 -- 2000 x 800 inner cells, 50-cell boundary, dx = dz = 5, dt = 4e-4,
+  nt = 5000; 30 horizontal layers with vp drawn uniformly in [1500, 4500]
+  and sorted to increase with depth, vs = vp / 1.73, rho = 310 vp^0.25
+  (Gardner), times a smooth Gaussian random field (sigma 5 %, correlation
+  length 40 cells); one dipping source (45 degrees), Ricker 15 Hz; 400
+  receivers along z = 5.
+"""
+import numpy as np
+
+
+def c0_params():
+    return dict(nt=4000, nx_inner=200, nz_inner=100, nx_inner_boundary=10, nz_inner_boundary=20,
+                dx=1.249, dz=1.249, dt=2.5e-4, np_boundary=25, np_factor=0.015,
+                scalar_rho=1500.0, scalar_vp=2000.0, scalar_vs=800.0, npx=1, npz=1,
+                peak_frequency=50.0, source_timeshift=0.0, delay_cycles_per_shot=24,
+                n_sources=2, ix_sources=[66, 133], iz_sources=[50, 50], moment_angles=[45.0, 60.0],
+                which_source_to_fire_in_which_shot=[[0, 1]], nr=19,
+                ix_receivers=[10 + 10 * k for k in range(19)], iz_receivers=[10] * 19,
+                snapshot_interval=10)
+
+
+def c0_media(seed=0):
+    p = c0_params()
+    nx, nz = p["nx_inner"] + 2 * p["np_boundary"], p["nz_inner"] + 2 * p["np_boundary"]
+    rng = np.random.default_rng(seed)
+    cx = p["np_boundary"] + rng.uniform(40, p["nx_inner"] - 40)
+    cz = p["np_boundary"] + rng.uniform(30, p["nz_inner"] - 30)
+    x = np.arange(nx)[:, None]
+    z = np.arange(nz)[None, :]
+    inside = ((x - cx) ** 2 + (z - cz) ** 2) < 15.0 ** 2
+    start = tuple(np.full((nx, nz), v) for v in (2000.0, 800.0, 1500.0))
+    target = tuple(a * (1 + 0.1 * inside) for a in start)
+    return target, start
+
+
+def c1_params(nt=5000):
+    n_rec = 400
+    return dict(nt=nt, nx_inner=2000, nz_inner=800, nx_inner_boundary=10, nz_inner_boundary=10,
+                dx=5.0, dz=5.0, dt=4e-4, np_boundary=50, np_factor=0.015,
+                scalar_rho=2000.0, scalar_vp=2500.0, scalar_vs=1445.0, npx=1, npz=1,
+                peak_frequency=15.0, source_timeshift=0.0, delay_cycles_per_shot=0,
+                n_sources=1, ix_sources=[1000], iz_sources=[10], moment_angles=[45.0],
+                which_source_to_fire_in_which_shot=[[0]], nr=n_rec,
+                ix_receivers=[2 + 5 * k for k in range(n_rec)], iz_receivers=[5] * n_rec,
+                snapshot_interval=10)
+
+
+def gaussian_random_field(shape, corr_len, sigma, rng):
+    """Zero-mean field with a Gaussian covariance of length `corr_len`
+    cells and standard deviation `sigma` (FFT-filtered white noise)."""
+    noise = rng.standard_normal(shape)
+    kx = np.fft.fftfreq(shape[0])[:, None]
+    kz = np.fft.rfftfreq(shape[1])[None, :]
+    filt = np.exp(-2.0 * (np.pi * corr_len) ** 2 * (kx ** 2 + kz ** 2) / 2.0)
+    f = np.fft.irfft2(np.fft.rfft2(noise) * filt, s=shape)
+    f -= f.mean()
+    return f * (sigma / f.std())
+
+
+def layered_media(nx, nz, np_boundary, n_layers, seed, vp_range=(1500.0, 4500.0),
+                  sigma=0.05, corr_len=40.0):
+    rng = np.random.default_rng(seed)
+    vps = np.sort(rng.uniform(vp_range[0], vp_range[1], n_layers))
+    inner = nz - 2 * np_boundary
+    depth = np.clip(np.arange(nz) - np_boundary, 0, inner - 1)
+    layer = np.minimum((depth * n_layers) // inner, n_layers - 1)
+    vp = np.repeat(vps[layer][None, :], nx, axis=0)
+    vp = vp * (1.0 + gaussian_random_field((nx, nz), corr_len, sigma, rng))
+    vs = vp / 1.73
+    rho = 310.0 * vp ** 0.25
+    return vp, vs, rho
+
+
+def c1_media(seed=1):
+    p = c1_params()
+    nx, nz = p["nx_inner"] + 2 * p["np_boundary"], p["nz_inner"] + 2 * p["np_boundary"]
+    return layered_media(nx, nz, p["np_boundary"], 30, seed)
