@@ -228,7 +228,16 @@ int psv_device_bytes(const psv_model *m, size_t *bytes);
  * src/fdModel.cpp:545-549). */
 int psv_profile_forward(psv_model *m, int i_shot, int n_steps, double *per_step_ms,
                         double *kernel_ms, int max_kernels, int *n_kernels);
-const char *psv_step_kernel_name(int k);
+const char *psv_step_kernel_name(const psv_model *m, int k);
+
+/* Time-step kernel variant: PSV_VARIANT_FUSED (one launch per step over
+ * ping-pong buffers; FP32 only, the FP32 default) or PSV_VARIANT_TWO_KERNEL
+ * (separate stress and velocity launches, as the reference's two loop nests;
+ * the only FP64 variant). Results of the two FP32 variants agree to FP32
+ * rounding. No counterpart in the reference. */
+enum psv_variant { PSV_VARIANT_FUSED = 0, PSV_VARIANT_TWO_KERNEL = 1 };
+int psv_set_kernel_variant(psv_model *m, int variant);
+int psv_get_kernel_variant(const psv_model *m, int *variant);
 
 #ifdef __cplusplus
 }

@@ -109,7 +109,9 @@ _SIGNATURES = {
     "psv_get_kernels_device": [_vp, _vp, _vp, _vp],
     "psv_device_bytes": [_vp, ctypes.POINTER(ctypes.c_size_t)],
     "psv_profile_forward": [_vp, _c_int, _c_int, _dp, _dp, _c_int, _ip],
-    "psv_step_kernel_name": [_c_int],
+    "psv_step_kernel_name": [_vp, _c_int],
+    "psv_set_kernel_variant": [_vp, _c_int],
+    "psv_get_kernel_variant": [_vp, _ip],
 }
 _RESTYPES = {"psv_last_error": ctypes.c_char_p, "psv_step_kernel_name": ctypes.c_char_p}
 

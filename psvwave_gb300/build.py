@@ -19,7 +19,11 @@ LIB_NAME = "libpsvwave_gb300.so"
 LIB_PATH = os.path.join(BUILD, LIB_NAME)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
+# Host code never contracts a*b+c into a fused multiply-add (g++ does by
+# default on aarch64): the setup tables (Ricker wavelets, taper) must round
+# exactly as the reference's double code does.
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
+          "-ffp-contract=off", "-I", CSRC, "-I", INCLUDE]
 
 # (source, extra flags)
 UNITS = [

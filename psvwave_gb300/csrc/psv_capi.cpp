@@ -500,8 +500,20 @@ int psv_profile_forward(psv_model *m, int i_shot, int n_steps, double *per_step_
   });
 }
 
-const char *psv_step_kernel_name(int k) {
-  return (k >= 0 && k < psv::kKernelsPerStep) ? psv::step_kernel_name(k) : "";
+const char *psv_step_kernel_name(const psv_model *m, int k) {
+  if (!m) return "";
+  return m->impl.step_kernel_name(k);
+}
+
+int psv_set_kernel_variant(psv_model *m, int variant) {
+  return guarded([&] { M(m).set_variant(variant); });
+}
+
+int psv_get_kernel_variant(const psv_model *m, int *variant) {
+  return guarded([&] {
+    need(variant, "variant");
+    *variant = M(m).variant();
+  });
 }
 
 int psv_device_bytes(const psv_model *m, size_t *bytes) {

@@ -14,6 +14,7 @@
 #include <sstream>
 
 #include "../../include/psvwave.h"
+#include "psv_fast.hpp"
 
 namespace psv {
 
@@ -86,6 +87,7 @@ Model::Model(const Config &cfg, int precision, int device)
     throw Error(PSV_ERR_INVALID_ARGUMENT, "CUDA device index out of range");
   DeviceGuard guard(device_);
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  variant_ = prec_ == PSV_FP32 ? kFused : kTwoKernel;
   build_tables();
   allocate();
   // Homogeneous background medium (src/fdModel.cpp:249-261).
@@ -105,7 +107,7 @@ Model::Model(const Config &cfg, int precision, int device)
 
 Model::Model(const Model &o)
     : cfg_(o.cfg_), geo_(o.geo_), prec_(o.prec_), device_(o.device_), async_(o.async_),
-      misfit_(o.misfit_) {
+      misfit_(o.misfit_), variant_(o.variant_), cur_(o.cur_) {
   DeviceGuard guard(device_);
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   build_tables();
@@ -118,6 +120,7 @@ Model::Model(const Model &o)
     cuda_check(cudaMemcpy(d.get(), s.get(), s.bytes(), cudaMemcpyDeviceToDevice), "clone");
   };
   for (int k = 0; k < 5; ++k) copy(fields_[k], o.fields_[k]);
+  for (int k = 0; k < 5; ++k) copy(fields2_[k], o.fields2_[k]);
   copy(lm_, o.lm_);
   copy(la_, o.la_);
   copy(mu_, o.mu_);
@@ -199,6 +202,8 @@ void Model::build_tables() {
 void Model::allocate() {
   const size_t g = grid_size(), e = elem(), d = data_size();
   for (auto &f : fields_) f.allocate(g * e);
+  if (prec_ == PSV_FP32)
+    for (auto &f : fields2_) f.allocate(g * e);
   lm_.allocate(g * e);
   la_.allocate(g * e);
   mu_.allocate(g * e);
@@ -329,6 +334,7 @@ size_t Model::device_bytes() const {
   size_t total = 0;
   auto add = [&](const DeviceBuffer &b) { total += b.bytes(); };
   for (auto &b : fields_) add(b);
+  for (auto &b : fields2_) add(b);
   for (auto &b : accu_) add(b);
   for (auto &b : klame_) add(b);
   for (auto &b : kvel_) add(b);
@@ -417,10 +423,17 @@ void Model::forward_simulate(int shot, bool store, bool verbose, bool output_wav
   SolverArgs a = solver_args();
   const InjPlan &plan = plans_[shot];
   auto t0 = std::chrono::steady_clock::now();
+  void *second[5] = {fields2_[0].get(), fields2_[1].get(), fields2_[2].get(), fields2_[3].get(),
+                     fields2_[4].get()};
   auto run = [&](int it0, int it1, bool zero, bool fin) {
-    cudaError_t e = prec_ == PSV_FP64
-                        ? forward_f64(a, plan, shot, store, it0, it1, zero, fin, stream())
-                        : forward_f32(a, plan, shot, store, it0, it1, zero, fin, stream());
+    cudaError_t e;
+    if (prec_ == PSV_FP64)
+      e = forward_f64(a, plan, shot, store, it0, it1, zero, fin, stream());
+    else if (variant_ == kFused)
+      e = fast::forward(a, second, &cur_, plan, shot, store, it0, it1, zero, fin, stream());
+    else
+      e = forward_f32(a, plan, shot, store, it0, it1, zero, fin, stream());
+    if (zero && !(prec_ == PSV_FP32 && variant_ == kFused)) cur_ = 0;
     cuda_check(e, "forward_simulate");
   };
   if (!output_wavefields) {
@@ -448,21 +461,28 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
   if (shot < 0 || shot >= cfg_.n_shots) throw Error(PSV_ERR_INVALID_ARGUMENT, "i_shot out of range");
   if (n_steps <= 0 || n_steps > cfg_.nt) n_steps = cfg_.nt;
   DeviceGuard guard(device_);
-  const int per = kKernelsPerStep + 1;
+  const int kps = kernels_per_step();
+  const int per = kps + 1;
   std::vector<cudaEvent_t> ev(static_cast<size_t>(per) * n_steps);
   for (auto &e : ev) cuda_check(cudaEventCreate(&e), "cudaEventCreate");
   SolverArgs a = solver_args();
   a.events = ev.data();
-  cudaError_t err =
-      prec_ == PSV_FP64
-          ? forward_f64(a, plans_[shot], shot, false, 0, n_steps, true, false, stream())
-          : forward_f32(a, plans_[shot], shot, false, 0, n_steps, true, false, stream());
+  void *second[5] = {fields2_[0].get(), fields2_[1].get(), fields2_[2].get(), fields2_[3].get(),
+                     fields2_[4].get()};
+  cudaError_t err;
+  if (prec_ == PSV_FP64)
+    err = forward_f64(a, plans_[shot], shot, false, 0, n_steps, true, false, stream());
+  else if (variant_ == kFused)
+    err = fast::forward(a, second, &cur_, plans_[shot], shot, false, 0, n_steps, true, false,
+                        stream());
+  else
+    err = forward_f32(a, plans_[shot], shot, false, 0, n_steps, true, false, stream());
   cudaError_t sync = cudaStreamSynchronize(stream());
-  std::vector<double> sums(kKernelsPerStep, 0.0);
+  std::vector<double> sums(kps, 0.0);
   double total = 0;
   if (err == cudaSuccess && sync == cudaSuccess) {
     for (int s = 0; s < n_steps; ++s) {
-      for (int k = 0; k < kKernelsPerStep; ++k) {
+      for (int k = 0; k < kps; ++k) {
         float ms = 0;
         cudaEventElapsedTime(&ms, ev[per * s + k], ev[per * s + k + 1]);
         sums[k] += ms;
@@ -476,9 +496,31 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
   cuda_check(err, "profile_forward");
   cuda_check(sync, "profile_forward");
   if (per_step_ms) *per_step_ms = total / n_steps;
-  for (int k = 0; k < kKernelsPerStep && k < max_kernels; ++k)
+  for (int k = 0; k < kps && k < max_kernels; ++k)
     if (kernel_ms) kernel_ms[k] = sums[k] / n_steps;
-  return kKernelsPerStep;
+  return kps;
+}
+
+void Model::set_variant(int v) {
+  if (v != kFused && v != kTwoKernel) throw Error(PSV_ERR_INVALID_ARGUMENT, "unknown kernel variant");
+  if (prec_ == PSV_FP64 && v == kFused)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "the fused variant is FP32 only");
+  DeviceGuard guard(device_);
+  if (v != variant_ && cur_ == 1) {
+    // Bring the current state back into the primary buffers.
+    for (int f = 0; f < 5; ++f)
+      cuda_check(cudaMemcpyAsync(fields_[f].get(), fields2_[f].get(), fields_[f].bytes(),
+                                 cudaMemcpyDeviceToDevice, stream()),
+                 "set_variant");
+    cur_ = 0;
+  }
+  variant_ = v;
+  synchronize();
+}
+
+const char *Model::step_kernel_name(int k) const {
+  if (variant_ == kFused) return k == 0 ? "fused_step" : "";
+  return k == 0 ? "stress_step" : (k == 1 ? "velocity_step" : "");
 }
 
 void Model::adjoint_simulate(int shot, bool verbose) {
@@ -487,8 +529,17 @@ void Model::adjoint_simulate(int shot, bool verbose) {
   ensure_snapshots();
   SolverArgs a = solver_args();
   auto t0 = std::chrono::steady_clock::now();
-  cudaError_t e = prec_ == PSV_FP64 ? adjoint_f64(a, plans_[cfg_.n_shots], shot, stream())
-                                    : adjoint_f32(a, plans_[cfg_.n_shots], shot, stream());
+  void *second[5] = {fields2_[0].get(), fields2_[1].get(), fields2_[2].get(), fields2_[3].get(),
+                     fields2_[4].get()};
+  cudaError_t e;
+  if (prec_ == PSV_FP64) {
+    e = adjoint_f64(a, plans_[cfg_.n_shots], shot, stream());
+  } else if (variant_ == kFused) {
+    e = fast::adjoint(a, second, &cur_, plans_[cfg_.n_shots], shot, stream());
+  } else {
+    e = adjoint_f32(a, plans_[cfg_.n_shots], shot, stream());
+    cur_ = 0;
+  }
   cuda_check(e, "adjoint_simulate");
   finish("adjoint_simulate");
   if (verbose) {
@@ -725,16 +776,17 @@ void Model::get_snapshots(double *out[5]) {
 void Model::get_wavefields(double *out[5]) {
   DeviceGuard guard(device_);
   const size_t n = grid_size();
+  DeviceBuffer *cur = (prec_ == PSV_FP32 && cur_ == 1) ? fields2_ : fields_;
   DeviceBuffer tmp;
   if (prec_ != PSV_FP64) tmp.allocate(n * sizeof(double));
   for (int f = 0; f < 5; ++f) {
     if (!out[f]) continue;
     if (prec_ == PSV_FP64) {
-      cuda_check(cudaMemcpyAsync(out[f], fields_[f].get(), n * sizeof(double),
+      cuda_check(cudaMemcpyAsync(out[f], cur[f].get(), n * sizeof(double),
                                  cudaMemcpyDeviceToHost, stream()),
                  "get_wavefields");
     } else {
-      widen(n, fields_[f].get(), tmp.as<double>());
+      widen(n, cur[f].get(), tmp.as<double>());
       cuda_check(cudaMemcpyAsync(out[f], tmp.get(), n * sizeof(double), cudaMemcpyDeviceToHost,
                                  stream()),
                  "get_wavefields");

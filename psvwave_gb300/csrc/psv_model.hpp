@@ -111,6 +111,13 @@ class Model {
   void write_sources() const;
   void write_kernels();
 
+  // Time-step kernel variant (Variant in psv_solver.hpp); FP64 models only
+  // run kTwoKernel.
+  void set_variant(int v);
+  int variant() const { return variant_; }
+  int kernels_per_step() const { return variant_ == kFused ? 1 : 2; }
+  const char *step_kernel_name(int k) const;
+
   void set_stream(cudaStream_t s) { user_stream_ = s; }
   cudaStream_t stream() const { return user_stream_ ? user_stream_ : stream_; }
   void set_async(bool a) { async_ = a; }
@@ -146,8 +153,12 @@ class Model {
   std::vector<double> moment_;                          // [n_sources][2][2]
   std::vector<double> taper_tab_;                       // [np + 1]
 
+  int variant_ = kTwoKernel;
+  int cur_ = 0;  // fused variant: 0 = fields_ hold the current state, 1 = fields2_
+
   // Device arrays.
   DeviceBuffer fields_[5];                    // vx vz txx tzz txz   (T)
+  DeviceBuffer fields2_[5];                   // second set (fused variant)
   DeviceBuffer lm_, la_, mu_, b_;             // medium              (T)
   DeviceBuffer vp_, vs_, rho_;                // medium              (FP64)
   DeviceBuffer taper_tab_d_;                  // (T)

@@ -63,14 +63,15 @@ struct SolverArgs {
   double *k_lam = nullptr, *k_mu = nullptr, *k_rho = nullptr;
   // free region, absolute indices [fx0, fx1) x [fz0, fz1)
   int fx0 = 0, fx1 = 0, fz0 = 0, fz1 = 0;
-  // optional profiling: kKernelsPerStep + 1 events per forward time step,
+  // optional profiling: (launches per step + 1) events per forward time step,
   // recorded before each launch of the step and after the last one
   cudaEvent_t *events = nullptr;
 };
 
-// Launches per forward time step, in launch order, and their names.
-constexpr int kKernelsPerStep = 2;
-inline const char *step_kernel_name(int k) { return k == 0 ? "stress_step" : "velocity_step"; }
+// Time-step kernel variants. kTwoKernel: stress_step then velocity_step
+// (both precisions; the FP64 path always uses it). kFused: one fused_step
+// launch per time step over ping-pong buffers (FP32 only, the default).
+enum Variant { kFused = 0, kTwoKernel = 1 };
 
 // Precision-specific entry points (defined in psv_solver_f32.cu / _f64.cu).
 #define PSV_SOLVER_DECLS(SUFFIX)                                                          \
@@ -86,6 +87,11 @@ inline const char *step_kernel_name(int k) { return k == 0 ? "stress_step" : "ve
 PSV_SOLVER_DECLS(f32)
 PSV_SOLVER_DECLS(f64)
 #undef PSV_SOLVER_DECLS
+
+// Seismograms from raw FP32 receiver velocities (psv_solver_f32.cu).
+cudaError_t receiver_cumsum_f32(int nr, int nt, int n_steps, double dt, double dxdz,
+                                const float *raw_x, const float *raw_z, double *out_x,
+                                double *out_z, cudaStream_t s);
 
 // FP64 helpers (psv_aux.cu).
 cudaError_t misfit_l2(size_t n, double dt, const double *obs_ux, const double *syn_ux,

@@ -407,5 +407,19 @@ class fdModel:
         n = ctypes.c_int()
         _capi.check(self._lib.psv_profile_forward(self._h, int(i_shot), int(n_steps),
                                                   ctypes.byref(per_step), ks, 8, ctypes.byref(n)))
-        names = [self._lib.psv_step_kernel_name(k).decode() for k in range(n.value)]
+        names = [self._lib.psv_step_kernel_name(self._h, k).decode() for k in range(n.value)]
         return per_step.value, dict(zip(names, list(ks)[:n.value]))
+
+    VARIANTS = {"fused": 0, "two_kernel": 1}
+
+    @property
+    def kernel_variant(self):
+        """'fused' (one launch per step, FP32) or 'two_kernel' (stress and
+        velocity launches; the FP64 variant)."""
+        v = ctypes.c_int()
+        _capi.check(self._lib.psv_get_kernel_variant(self._h, ctypes.byref(v)))
+        return {0: "fused", 1: "two_kernel"}[v.value]
+
+    @kernel_variant.setter
+    def kernel_variant(self, name):
+        _capi.check(self._lib.psv_set_kernel_variant(self._h, self.VARIANTS[name]))

@@ -9,6 +9,8 @@ FP32 wave fields are held to the tolerance of the production path: relative
 L2 error <= 1e-4 against the FP64 answer for seismograms, misfit, adjoint
 sources, kernels and the gradient vector.
 """
+import platform
+
 import numpy as np
 import pytest
 
@@ -34,26 +36,62 @@ def gpu_outputs(m):
     return dict(zip(OUTPUTS, (ux, uz, au, az, lk, mk, rk, vk, sk, dk)))
 
 
+# The golden fixtures were made on x86-64. Where the GPU host is another
+# architecture, its libm may round exp/sin/cos of the setup tables (Ricker
+# wavelet, moment tensor, taper) differently in the last bit, so there the
+# comparison with the fixtures is held to 1e-10 relative L2, and bit-exactness
+# is asserted against the oracle port built on the same machine instead.
+SAME_ARCH_AS_GOLDEN = platform.machine() in ("x86_64", "AMD64")
+
+
+def assert_golden(a, b, name):
+    if SAME_ARCH_AS_GOLDEN:
+        assert np.array_equal(a, b), (name, rel_l2(a, b))
+    else:
+        assert rel_l2(a, b) <= 1e-10, (name, rel_l2(a, b))
+
+
 def test_setup_tables_bit_exact(golden):
     m = psv.fdModel(SMALL_INI, precision="fp64")
-    assert np.array_equal(m.get_taper(), golden["taper"])
-    assert np.array_equal(m.get_stf(), golden["stf"])
-    assert np.array_equal(m.get_moment(), golden["moment"])
+    o = portbind.OracleModel(SMALL_INI)
+    assert np.array_equal(m.get_taper(), o.array("taper"))
+    assert np.array_equal(m.get_stf(), o.array("stf"))
+    assert np.array_equal(m.get_moment(), o.array("moment"))
+    for name in ("taper", "stf", "moment"):
+        assert_golden(getattr(m, "get_" + name)(), golden[name], name)
 
 
-def test_fp64_gradient_bit_exact_vs_reference(golden):
+def test_fp64_gradient_vs_reference_golden(golden):
     m = psv.fdModel(SMALL_INI, precision="fp64")
     misfit = fwi_gradient(m, tuple(golden["target"]), tuple(golden["start"]))
     assert abs(misfit - golden["misfit"]) <= MISFIT_FP64_TOL * golden["misfit"]
     out = gpu_outputs(m)
     for name in OUTPUTS:
-        assert np.array_equal(out[name], golden[name]), (name, rel_l2(out[name], golden[name]))
-    assert np.array_equal(m.get_observed_data()[0], golden["obs_ux"])
+        assert_golden(out[name], golden[name], name)
+    assert_golden(m.get_observed_data()[0], golden["obs_ux"], "obs")
     assert np.array_equal(m.get_model_vector(), golden["model_vector"])
-    assert np.array_equal(m.get_gradient_vector(), golden["gradient_vector"])
+    assert_golden(m.get_gradient_vector(), golden["gradient_vector"], "gradient")
     snaps = m.get_snapshots()
-    assert np.array_equal(np.stack([s[1, 25] for s in snaps]), golden["snap_shot1_25"])
-    assert np.array_equal(np.stack(m.get_wavefields()), golden["adjoint_fields"])
+    assert_golden(np.stack([s[1, 25] for s in snaps]), golden["snap_shot1_25"], "snapshot")
+    assert_golden(np.stack(m.get_wavefields()), golden["adjoint_fields"], "adjoint fields")
+
+
+def test_fp64_gradient_bit_exact_vs_oracle_same_machine(golden):
+    o = portbind.OracleModel(SMALL_INI)
+    m = psv.fdModel(SMALL_INI, precision="fp64")
+    mo = fwi_gradient(o, tuple(golden["target"]), tuple(golden["start"]))
+    mg = fwi_gradient(m, tuple(golden["target"]), tuple(golden["start"]))
+    assert abs(mg - mo) <= MISFIT_FP64_TOL * mo
+    out = gpu_outputs(m)
+    for name in OUTPUTS:
+        assert np.array_equal(out[name], o.array(name)), (name, rel_l2(out[name], o.array(name)))
+    assert np.array_equal(m.get_gradient_vector(), o.get_gradient_vector())
+    snaps = m.get_snapshots()
+    for k, n in enumerate(("accu_vx", "accu_vz", "accu_txx", "accu_tzz", "accu_txz")):
+        assert np.array_equal(snaps[k], o.array(n)), n
+    fields = m.get_wavefields()
+    for k, n in enumerate(("vx", "vz", "txx", "tzz", "txz")):
+        assert np.array_equal(fields[k], o.array(n)), n
 
 
 def test_fp64_matches_oracle_port_on_seeded_case():
@@ -115,3 +153,37 @@ def test_fp32_vs_fp64_gpu_nb2_full_outputs():
     print("NB2 fp32 vs fp64:", errs)
     for k, e in errs.items():
         assert e <= FP32_TOL, (k, e)
+
+
+@pytest.mark.parametrize("variant", ["fused", "two_kernel"])
+def test_fp32_variants_within_tolerance(golden, variant):
+    m = psv.fdModel(SMALL_INI, precision="fp32")
+    m.kernel_variant = variant
+    assert m.kernel_variant == variant
+    fwi_gradient(m, tuple(golden["target"]), tuple(golden["start"]))
+    out = gpu_outputs(m)
+    for name in OUTPUTS:
+        assert rel_l2(out[name], golden[name]) <= FP32_TOL, name
+
+
+def test_fp32_fused_vs_two_kernel_agree():
+    """The two FP32 kernel variants agree to FP32 rounding (5000 steps on the
+    Notebook 2 grid, seismograms and final wave fields)."""
+    res = []
+    for variant in ("fused", "two_kernel"):
+        m = psv.fdModel(NB2_INI, precision="fp32")
+        m.kernel_variant = variant
+        target, _ = nb2_media(m.nx, m.nz, m.np_boundary, m.dx, m.dz)
+        m.set_parameter_fields(*target)
+        m.forward_simulate(0, False)
+        res.append((m.get_synthetic_data(), m.get_wavefields()))
+    for a, b in zip(res[0][0], res[1][0]):
+        assert rel_l2(a, b) <= 1e-5
+    for a, b in zip(res[0][1], res[1][1]):
+        assert rel_l2(a, b) <= 1e-4
+
+
+def test_fp64_rejects_fused_variant():
+    m = psv.fdModel(SMALL_INI, precision="fp64")
+    with pytest.raises(ValueError):
+        m.kernel_variant = "fused"
