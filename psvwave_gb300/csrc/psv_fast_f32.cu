@@ -93,103 +93,156 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
   }
 
   // Phase A: old velocities over the tile + 4-point halo (zero outside).
-  for (int e = threadIdx.x; e < VXD * VZD; e += NT) {
-    const int lx = e / VZD, lz = e - lx * VZD;
-    const int gx = X0 - 4 + lx, gz = Z0 - 4 + lz;
-    float vx = 0.f, vz = 0.f;
-    if (gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
-      const size_t g = (size_t)gx * nz + gz;
-      vx = a.in.vx[g];
-      vz = a.in.vz[g];
+  // All of a thread's loads are issued before any is stored, so they are in
+  // flight together.
+  {
+    constexpr int N = VXD * VZD, K = (N + NT - 1) / NT;
+    float rx[K], rz[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int e = threadIdx.x + k * NT;
+      const int lx = e / VZD, lz = e - lx * VZD;
+      const int gx = X0 - 4 + lx, gz = Z0 - 4 + lz;
+      rx[k] = 0.f;
+      rz[k] = 0.f;
+      if (e < N && gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
+        const size_t g = (size_t)gx * nz + gz;
+        rx[k] = __ldg(a.in.vx + g);
+        rz[k] = __ldg(a.in.vz + g);
+      }
     }
-    sv[0][lx][lz] = vx;
-    sv[1][lx][lz] = vz;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int e = threadIdx.x + k * NT;
+      if (e < N) {
+        const int lx = e / VZD, lz = e - lx * VZD;
+        sv[0][lx][lz] = rx[k];
+        sv[1][lx][lz] = rz[k];
+      }
+    }
   }
   __syncthreads();
 
-  // Phase B: new stresses over the tile + 2-point halo.
-  for (int e = threadIdx.x; e < SXD * SZD; e += NT) {
-    const int lx = e / SZD, lz = e - lx * SZD;
-    const int gx = X0 - 2 + lx, gz = Z0 - 2 + lz;
-    float txx = 0.f, tzz = 0.f, txz = 0.f;
-    if (gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
-      const size_t g = (size_t)gx * nz + gz;
-      txx = a.in.txx[g];
-      tzz = a.in.tzz[g];
-      txz = a.in.txz[g];
-      const bool own = lx >= 2 && lx < TX + 2 && lz >= 2 && lz < TZ + 2;
-      const int vx_ = lx + 2, vz_ = lz + 2;  // this point in the velocity tile
-      if (own && a.snap[0]) {
-        a.snap[0][g] = sv[0][vx_][vz_];
-        a.snap[1][g] = sv[1][vx_][vz_];
-        a.snap[2][g] = txx;
-        a.snap[3][g] = tzz;
-        a.snap[4][g] = txz;
+  // Phase B: new stresses over the tile + 2-point halo, in chunks of CH
+  // points per thread whose loads are issued together.
+  {
+    constexpr int N = SXD * SZD, K = (N + NT - 1) / NT, CH = ADJ ? 3 : 5;
+    const float(*VX)[VZD] = sv[0];
+    const float(*VZ)[VZD] = sv[1];
+#pragma unroll
+    for (int k0 = 0; k0 < K; k0 += CH) {
+      float txx[CH], tzz[CH], txz[CH], lm[CH], la[CH], mu[CH];
+#pragma unroll
+      for (int j = 0; j < CH; ++j) {
+        const int e = threadIdx.x + (k0 + j) * NT;
+        const int lx = e / SZD, lz = e - lx * SZD;
+        const int gx = X0 - 2 + lx, gz = Z0 - 2 + lz;
+        txx[j] = tzz[j] = txz[j] = 0.f;
+        lm[j] = la[j] = mu[j] = 0.f;
+        if (k0 + j < K && e < N && gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
+          const size_t g = (size_t)gx * nz + gz;
+          txx[j] = __ldg(a.in.txx + g);
+          tzz[j] = __ldg(a.in.tzz + g);
+          txz[j] = __ldg(a.in.txz + g);
+          lm[j] = __ldg(a.lm + g);
+          la[j] = __ldg(a.la + g);
+          mu[j] = __ldg(a.mu + g);
+        }
       }
-      if (ADJ && own && a.asnap[0] && gx >= a.fx0 && gx < a.fx1 && gz >= a.fz0 && gz < a.fz1)
-        correlate(a, g, sv[0][vx_][vz_], sv[1][vx_][vz_], txx, tzz, txz);
-      if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
-        const float(*VX)[VZD] = sv[0];
-        const float(*VZ)[VZD] = sv[1];
-        const float dvx = c1 * (VX[vx_ + 1][vz_] - VX[vx_][vz_]) +
-                          c2 * (VX[vx_ - 1][vz_] - VX[vx_ + 2][vz_]);
-        const float dvz = c1 * (VZ[vx_][vz_] - VZ[vx_][vz_ - 1]) +
-                          c2 * (VZ[vx_][vz_ - 2] - VZ[vx_][vz_ + 1]);
-        const float sxz = (c1 * (VX[vx_][vz_ + 1] - VX[vx_][vz_]) +
-                           c2 * (VX[vx_][vz_ - 1] - VX[vx_][vz_ + 2])) * a.idz +
-                          (c1 * (VZ[vx_][vz_] - VZ[vx_ - 1][vz_]) +
-                           c2 * (VZ[vx_ - 2][vz_] - VZ[vx_ + 1][vz_])) * a.idx;
-        const float lm = a.lm[g], la = a.la[g], mu = a.mu[g];
-        const float ex = dvx * a.idx, ez = dvz * a.idz;
-        const float tp = taper(a, gx, gz);
-        const float dt = ADJ ? -a.dt : a.dt;
-        txx = tp * (txx + dt * (lm * ex + la * ez));
-        tzz = tp * (tzz + dt * (la * ex + lm * ez));
-        txz = tp * (txz + dt * mu * sxz);
-      }
-      if (own) {
-        a.out.txx[g] = txx;
-        a.out.tzz[g] = tzz;
-        a.out.txz[g] = txz;
+#pragma unroll
+      for (int j = 0; j < CH; ++j) {
+        const int e = threadIdx.x + (k0 + j) * NT;
+        if (k0 + j >= K || e >= N) continue;
+        const int lx = e / SZD, lz = e - lx * SZD;
+        const int gx = X0 - 2 + lx, gz = Z0 - 2 + lz;
+        float sxx = txx[j], szz = tzz[j], sxz = txz[j];
+        if (gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
+          const size_t g = (size_t)gx * nz + gz;
+          const bool own = lx >= 2 && lx < TX + 2 && lz >= 2 && lz < TZ + 2;
+          const int vx_ = lx + 2, vz_ = lz + 2;  // this point in the velocity tile
+          if (own && a.snap[0]) {
+            a.snap[0][g] = VX[vx_][vz_];
+            a.snap[1][g] = VZ[vx_][vz_];
+            a.snap[2][g] = sxx;
+            a.snap[3][g] = szz;
+            a.snap[4][g] = sxz;
+          }
+          if (ADJ && own && a.asnap[0] && gx >= a.fx0 && gx < a.fx1 && gz >= a.fz0 &&
+              gz < a.fz1)
+            correlate(a, g, VX[vx_][vz_], VZ[vx_][vz_], sxx, szz, sxz);
+          if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
+            const float dvx = c1 * (VX[vx_ + 1][vz_] - VX[vx_][vz_]) +
+                              c2 * (VX[vx_ - 1][vz_] - VX[vx_ + 2][vz_]);
+            const float dvz = c1 * (VZ[vx_][vz_] - VZ[vx_][vz_ - 1]) +
+                              c2 * (VZ[vx_][vz_ - 2] - VZ[vx_][vz_ + 1]);
+            const float gxz = (c1 * (VX[vx_][vz_ + 1] - VX[vx_][vz_]) +
+                               c2 * (VX[vx_][vz_ - 1] - VX[vx_][vz_ + 2])) * a.idz +
+                              (c1 * (VZ[vx_][vz_] - VZ[vx_ - 1][vz_]) +
+                               c2 * (VZ[vx_ - 2][vz_] - VZ[vx_ + 1][vz_])) * a.idx;
+            const float ex = dvx * a.idx, ez = dvz * a.idz;
+            const float tp = taper(a, gx, gz);
+            const float dt = ADJ ? -a.dt : a.dt;
+            sxx = tp * (sxx + dt * (lm[j] * ex + la[j] * ez));
+            szz = tp * (szz + dt * (la[j] * ex + lm[j] * ez));
+            sxz = tp * (sxz + dt * mu[j] * gxz);
+          }
+          if (own) {
+            a.out.txx[g] = sxx;
+            a.out.tzz[g] = szz;
+            a.out.txz[g] = sxz;
+          }
+        }
+        st[0][lx][lz] = sxx;
+        st[1][lx][lz] = szz;
+        st[2][lx][lz] = sxz;
       }
     }
-    st[0][lx][lz] = txx;
-    st[1][lx][lz] = tzz;
-    st[2][lx][lz] = txz;
   }
   __syncthreads();
 
   // Phase C: new velocities of the tile's own points.
-  const float(*TXX)[SZD] = st[0];
-  const float(*TZZ)[SZD] = st[1];
-  const float(*TXZ)[SZD] = st[2];
-  const InjPlan &p = a.plan;
-  for (int e = threadIdx.x; e < TX * TZ; e += NT) {
-    const int lx = e / TZ, lz = e % TZ;
-    const int gx = X0 + lx, gz = Z0 + lz;
-    if (gx >= nx || gz >= nz) continue;
-    const size_t g = (size_t)gx * nz + gz;
-    float vx = sv[0][lx + 4][lz + 4], vz = sv[1][lx + 4][lz + 4];
-    const float b = a.b[g];
-    if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
-      const int sx = lx + 2, sz = lz + 2;
-      const float ax = (c1 * (TXX[sx][sz] - TXX[sx - 1][sz]) +
-                        c2 * (TXX[sx - 2][sz] - TXX[sx + 1][sz])) * a.idx +
-                       (c1 * (TXZ[sx][sz] - TXZ[sx][sz - 1]) +
-                        c2 * (TXZ[sx][sz - 2] - TXZ[sx][sz + 1])) * a.idz;
-      const float az = (c1 * (TXZ[sx + 1][sz] - TXZ[sx][sz]) +
-                        c2 * (TXZ[sx - 1][sz] - TXZ[sx + 2][sz])) * a.idx +
-                       (c1 * (TZZ[sx][sz + 1] - TZZ[sx][sz]) +
-                        c2 * (TZZ[sx][sz - 1] - TZZ[sx][sz + 2])) * a.idz;
-      const float tp = taper(a, gx, gz);
-      const float bdt = b * (ADJ ? -a.dt : a.dt);
-      vx = tp * (vx + bdt * ax);
-      vz = tp * (vz + bdt * az);
+  {
+    constexpr int K = TX * TZ / NT;
+    const float(*TXX)[SZD] = st[0];
+    const float(*TZZ)[SZD] = st[1];
+    const float(*TXZ)[SZD] = st[2];
+    const InjPlan &p = a.plan;
+    float bb[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int e = threadIdx.x + k * NT;
+      const int gx = X0 + e / TZ, gz = Z0 + e % TZ;
+      bb[k] = (gx < nx && gz < nz) ? __ldg(a.b + (size_t)gx * nz + gz) : 0.f;
     }
-    if (p.n && gx >= p.x0 && gx < p.x0 + p.w && gz >= p.z0 && gz < p.z0 + p.h)
-      inject(a, g, gx, gz, b, vx, vz);
-    a.out.vx[g] = vx;
-    a.out.vz[g] = vz;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int e = threadIdx.x + k * NT;
+      const int lx = e / TZ, lz = e % TZ;
+      const int gx = X0 + lx, gz = Z0 + lz;
+      if (gx >= nx || gz >= nz) continue;
+      const size_t g = (size_t)gx * nz + gz;
+      float vx = sv[0][lx + 4][lz + 4], vz = sv[1][lx + 4][lz + 4];
+      const float b = bb[k];
+      if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
+        const int sx = lx + 2, sz = lz + 2;
+        const float ax = (c1 * (TXX[sx][sz] - TXX[sx - 1][sz]) +
+                          c2 * (TXX[sx - 2][sz] - TXX[sx + 1][sz])) * a.idx +
+                         (c1 * (TXZ[sx][sz] - TXZ[sx][sz - 1]) +
+                          c2 * (TXZ[sx][sz - 2] - TXZ[sx][sz + 1])) * a.idz;
+        const float az = (c1 * (TXZ[sx + 1][sz] - TXZ[sx][sz]) +
+                          c2 * (TXZ[sx - 1][sz] - TXZ[sx + 2][sz])) * a.idx +
+                         (c1 * (TZZ[sx][sz + 1] - TZZ[sx][sz]) +
+                          c2 * (TZZ[sx][sz - 1] - TZZ[sx][sz + 2])) * a.idz;
+        const float tp = taper(a, gx, gz);
+        const float bdt = b * (ADJ ? -a.dt : a.dt);
+        vx = tp * (vx + bdt * ax);
+        vz = tp * (vz + bdt * az);
+      }
+      if (p.n && gx >= p.x0 && gx < p.x0 + p.w && gz >= p.z0 && gz < p.z0 + p.h)
+        inject(a, g, gx, gz, b, vx, vz);
+      a.out.vx[g] = vx;
+      a.out.vz[g] = vz;
+    }
   }
 }
 

@@ -167,16 +167,18 @@ def test_fp32_variants_within_tolerance(golden, variant):
 
 
 def test_fp32_fused_vs_two_kernel_agree():
-    """The two FP32 kernel variants agree to FP32 rounding (5000 steps on the
-    Notebook 2 grid, seismograms and final wave fields)."""
+    """The two FP32 kernel variants agree to FP32 rounding on the 8000-step
+    Notebook 2 run: seismograms within 1e-5, and the stored wave fields at
+    four instants while the wave is in the grid within 1e-4."""
     res = []
     for variant in ("fused", "two_kernel"):
         m = psv.fdModel(NB2_INI, precision="fp32")
         m.kernel_variant = variant
         target, _ = nb2_media(m.nx, m.nz, m.np_boundary, m.dx, m.dz)
         m.set_parameter_fields(*target)
-        m.forward_simulate(0, False)
-        res.append((m.get_synthetic_data(), m.get_wavefields()))
+        m.forward_simulate(0, True)
+        snaps = m.get_snapshots()
+        res.append((m.get_synthetic_data(), [s[0, [100, 200, 400, 600]] for s in snaps]))
     for a, b in zip(res[0][0], res[1][0]):
         assert rel_l2(a, b) <= 1e-5
     for a, b in zip(res[0][1], res[1][1]):
