@@ -239,6 +239,26 @@ enum psv_variant { PSV_VARIANT_FUSED = 0, PSV_VARIANT_TWO_KERNEL = 1 };
 int psv_set_kernel_variant(psv_model *m, int variant);
 int psv_get_kernel_variant(const psv_model *m, int *variant);
 
+/* ---- no-allocation entry point ------------------------------------------ */
+/* L2 misfit 0.5 dt sum((obs - syn)^2) over both components, written to the
+ * device double *misfit, from caller-owned device arrays of n samples each
+ * (e.g. n_shots * nr * nt), on `stream` (a cudaStream_t; NULL = the legacy
+ * default stream). No counterpart in the reference: it is the same
+ * reduction as psv_calculate_l2_misfit, for callers that cannot allocate
+ * device memory (a TensorRT plugin's enqueue, an XLA custom call, a
+ * pre-planned memory arena, a region being captured into a CUDA graph).
+ * It allocates nothing: its partial sums live in a fixed 64 KiB __device__
+ * array that every GPU loading this library holds until exit, so n is
+ * limited to 16,777,216 samples; larger n returns PSV_ERR_INVALID_ARGUMENT.
+ * The first call on a device (made current by the caller) looks up that
+ * array's address; make that first call before any stream capture. All calls
+ * share the array: calls that overlap on the GPU race and must be ordered
+ * (one stream, or events) by the caller. Asynchronous: the result is ready
+ * when `stream` reaches it. */
+int psv_l2_misfit_noalloc(const double *obs_ux, const double *syn_ux, const double *obs_uz,
+                          const double *syn_uz, size_t n, double dt, double *misfit,
+                          void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -112,6 +112,7 @@ _SIGNATURES = {
     "psv_step_kernel_name": [_vp, _c_int],
     "psv_set_kernel_variant": [_vp, _c_int],
     "psv_get_kernel_variant": [_vp, _ip],
+    "psv_l2_misfit_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_size_t, _c_double, _vp, _vp],
 }
 _RESTYPES = {"psv_last_error": ctypes.c_char_p, "psv_step_kernel_name": ctypes.c_char_p}
 

@@ -31,6 +31,7 @@ UNITS = [
     ("psv_solver_f32.cu", []),
     ("psv_fast_f32.cu", []),
     ("psv_aux.cu", ["-fmad=false"]),
+    ("psv_noalloc.cu", []),
     ("psv_config.cpp", []),
     ("psv_model.cpp", []),
     ("psv_capi.cpp", []),

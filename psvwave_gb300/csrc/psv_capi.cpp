@@ -524,3 +524,8 @@ int psv_device_bytes(const psv_model *m, size_t *bytes) {
 }
 
 }  // extern "C"
+
+namespace psv {
+// Lets other translation units report through psv_last_error().
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace psv
