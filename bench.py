@@ -28,7 +28,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Gcell-updates/s"
-BYTES_PER_CELL = {"stress_step": 48, "velocity_step": 36, "fused_step": 56}  # FP32 algorithmic bytes per cell
+# FP32 algorithmic bytes per cell-update of each step kernel
+BYTES_PER_CELL = {"stress_step": 48, "velocity_step": 36, "fused_step": 56, "fused_step_tma": 52}
 
 
 def parse():

@@ -233,9 +233,11 @@ const char *psv_step_kernel_name(const psv_model *m, int k);
 /* Time-step kernel variant: PSV_VARIANT_FUSED (one launch per step over
  * ping-pong buffers; FP32 only, the FP32 default) or PSV_VARIANT_TWO_KERNEL
  * (separate stress and velocity launches, as the reference's two loop nests;
- * the only FP64 variant). Results of the two FP32 variants agree to FP32
- * rounding. No counterpart in the reference. */
-enum psv_variant { PSV_VARIANT_FUSED = 0, PSV_VARIANT_TWO_KERNEL = 1 };
+ * the only FP64 variant) or PSV_VARIANT_FUSED_TMA (the fused step with TMA
+ * tile loads; FP32 grids with nz % 4 == 0, where it is the default). Results
+ * of the FP32 variants agree to FP32 rounding. No counterpart in the
+ * reference. */
+enum psv_variant { PSV_VARIANT_FUSED = 0, PSV_VARIANT_TWO_KERNEL = 1, PSV_VARIANT_FUSED_TMA = 2 };
 int psv_set_kernel_variant(psv_model *m, int variant);
 int psv_get_kernel_variant(const psv_model *m, int *variant);
 

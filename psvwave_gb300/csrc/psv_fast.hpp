@@ -41,6 +41,12 @@ struct StepArgs {
 
 cudaError_t step(const StepArgs &a, bool adjoint, cudaStream_t s);
 
+// StepArgs fields that do not change within a simulation.
+StepArgs base_step_args(const SolverArgs &a);
+// Points in/out at the buffer set holding the current state (cur: 0 =
+// primary, 1 = second) and at the other one.
+void set_step_buffers(StepArgs &s, const SolverArgs &a, void *const second[5], int cur);
+
 // Time loops over two buffer sets: `primary` = the SolverArgs fields,
 // `second` = the other set. *cur (0 = primary, 1 = second) names the set that
 // holds the current state and is updated as the loop swaps them. Events, if

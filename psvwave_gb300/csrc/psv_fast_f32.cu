@@ -265,7 +265,20 @@ cudaError_t launch(const StepArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-StepArgs base_args(const SolverArgs &a) {
+cudaError_t zero(const SolverArgs &a, void *const second[5], cudaStream_t s) {
+  const size_t bytes = (size_t)a.nx * a.nz * sizeof(float);
+  void *prim[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
+  for (int f = 0; f < 5; ++f) {
+    cudaError_t e = cudaMemsetAsync(prim[f], 0, bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(second[f], 0, bytes, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
+StepArgs base_step_args(const SolverArgs &a) {
   StepArgs s;
   s.nx = a.nx;
   s.nz = a.nz;
@@ -283,7 +296,7 @@ StepArgs base_args(const SolverArgs &a) {
   return s;
 }
 
-void set_buffers(StepArgs &s, const SolverArgs &a, void *const second[5], int cur) {
+void set_step_buffers(StepArgs &s, const SolverArgs &a, void *const second[5], int cur) {
   void *prim[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
   void *const *src = cur == 0 ? prim : second;
   void *const *dst = cur == 0 ? second : prim;
@@ -292,19 +305,6 @@ void set_buffers(StepArgs &s, const SolverArgs &a, void *const second[5], int cu
   s.out = Fields{(float *)dst[0], (float *)dst[1], (float *)dst[2], (float *)dst[3],
                  (float *)dst[4]};
 }
-
-cudaError_t zero(const SolverArgs &a, void *const second[5], cudaStream_t s) {
-  const size_t bytes = (size_t)a.nx * a.nz * sizeof(float);
-  void *prim[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
-  for (int f = 0; f < 5; ++f) {
-    cudaError_t e = cudaMemsetAsync(prim[f], 0, bytes, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(second[f], 0, bytes, s);
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
-}
-
-}  // namespace
 
 cudaError_t step(const StepArgs &a, bool adjoint, cudaStream_t s) {
   return adjoint ? launch<true>(a, s) : launch<false>(a, s);
@@ -318,7 +318,7 @@ cudaError_t forward(const SolverArgs &a, void *const second[5], int *cur, const 
     if (e != cudaSuccess) return e;
     *cur = 0;
   }
-  StepArgs sa = base_args(a);
+  StepArgs sa = base_step_args(a);
   sa.plan = plan;
   sa.stf = a.stf;
   sa.rec_cell = a.rec_cell;
@@ -333,7 +333,7 @@ cudaError_t forward(const SolverArgs &a, void *const second[5], int *cur, const 
       sa.snap[f] = (store && it % a.si == 0)
                        ? (float *)a.accu[f] + ((size_t)shot * a.snapshots + it / a.si) * gsz
                        : nullptr;
-    set_buffers(sa, a, second, *cur);
+    set_step_buffers(sa, a, second, *cur);
     cudaEvent_t *ev = a.events ? a.events + 2 * (it - it0) : nullptr;
     if (ev) cudaEventRecord(ev[0], s);
     cudaError_t e = launch<false>(sa, s);
@@ -354,7 +354,7 @@ cudaError_t adjoint(const SolverArgs &a, void *const second[5], int *cur, const 
   cudaError_t e = zero(a, second, s);
   if (e != cudaSuccess) return e;
   *cur = 0;
-  StepArgs sa = base_args(a);
+  StepArgs sa = base_step_args(a);
   sa.plan = plan;
   sa.a_ux = a.a_stf_ux + (size_t)shot * a.nr * a.nt;
   sa.a_uz = a.a_stf_uz + (size_t)shot * a.nr * a.nt;
@@ -373,7 +373,7 @@ cudaError_t adjoint(const SolverArgs &a, void *const second[5], int *cur, const 
       sa.asnap[f] = (it % a.si == 0)
                         ? (const float *)a.accu[f] + ((size_t)shot * a.snapshots + it / a.si) * gsz
                         : nullptr;
-    set_buffers(sa, a, second, *cur);
+    set_step_buffers(sa, a, second, *cur);
     e = launch<true>(sa, s);
     if (e != cudaSuccess) return e;
     *cur ^= 1;

@@ -90,6 +90,8 @@ Model::Model(const Config &cfg, int precision, int device)
   variant_ = prec_ == PSV_FP32 ? kFused : kTwoKernel;
   build_tables();
   allocate();
+  build_tma_maps();
+  if (tma_ok_) variant_ = kFusedTma;
   // Homogeneous background medium (src/fdModel.cpp:249-261).
   std::vector<double> v(grid_size());
   const double scal[3] = {cfg_.scalar_vp, cfg_.scalar_vs, cfg_.scalar_rho};
@@ -112,6 +114,7 @@ Model::Model(const Model &o)
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   build_tables();
   allocate();
+  build_tma_maps();
   build_plans();
   const_cast<Model &>(o).synchronize();
   auto copy = [&](DeviceBuffer &d, const DeviceBuffer &s) {
@@ -221,6 +224,7 @@ void Model::allocate() {
   for (auto &k : klame_) k.allocate(g * sizeof(double));
   for (auto &k : kvel_) k.allocate(g * sizeof(double));
   partials_.allocate(kPartials * sizeof(double));
+  err_flag_.allocate(sizeof(int));
   scalar_.allocate(sizeof(double));
   stf_d_.allocate(stf_.size() * sizeof(double));
   if (!stf_.empty())
@@ -321,6 +325,30 @@ void Model::build_plans() {
       plan.map = plan_maps_[p].as<int>();
     }
     plans_[p] = plan;
+  }
+}
+
+void Model::build_tma_maps() {
+  tma_ok_ = false;
+  if (prec_ != PSV_FP32 || !tma::supported(geo_.nx, geo_.nz)) return;
+  const float *a[5], *b[5];
+  for (int f = 0; f < 5; ++f) {
+    a[f] = fields_[f].as<float>();
+    b[f] = fields2_[f].as<float>();
+  }
+  tma_ok_ = tma::make_maps(maps_[0], a, lm_.as<float>(), mu_.as<float>(), geo_.nx, geo_.nz) &&
+            tma::make_maps(maps_[1], b, lm_.as<float>(), mu_.as<float>(), geo_.nx, geo_.nz);
+}
+
+void Model::check_device_error() {
+  int flag = 0;
+  cuda_check(cudaMemcpyAsync(&flag, err_flag_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream()),
+             "error flag");
+  cuda_check(cudaStreamSynchronize(stream()), "error flag");
+  if (flag) {
+    cudaMemsetAsync(err_flag_.get(), 0, sizeof(int), stream());
+    cudaStreamSynchronize(stream());
+    throw Error(PSV_ERR_CUDA, "a CTA timed out waiting for its TMA tile copies");
   }
 }
 
@@ -429,11 +457,14 @@ void Model::forward_simulate(int shot, bool store, bool verbose, bool output_wav
     cudaError_t e;
     if (prec_ == PSV_FP64)
       e = forward_f64(a, plan, shot, store, it0, it1, zero, fin, stream());
+    else if (variant_ == kFusedTma)
+      e = tma::forward(a, second, &cur_, maps_, err_flag_.as<int>(), plan, shot, store, it0, it1,
+                       zero, fin, stream());
     else if (variant_ == kFused)
       e = fast::forward(a, second, &cur_, plan, shot, store, it0, it1, zero, fin, stream());
     else
       e = forward_f32(a, plan, shot, store, it0, it1, zero, fin, stream());
-    if (zero && !(prec_ == PSV_FP32 && variant_ == kFused)) cur_ = 0;
+    if (zero && (prec_ == PSV_FP64 || variant_ == kTwoKernel)) cur_ = 0;
     cuda_check(e, "forward_simulate");
   };
   if (!output_wavefields) {
@@ -449,6 +480,7 @@ void Model::forward_simulate(int shot, bool store, bool verbose, bool output_wav
     run(n_steps, n_steps, false, true);
   }
   finish("forward_simulate");
+  if (!async_ && variant_ == kFusedTma) check_device_error();
   if (verbose) {
     synchronize();
     double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -472,6 +504,9 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
   cudaError_t err;
   if (prec_ == PSV_FP64)
     err = forward_f64(a, plans_[shot], shot, false, 0, n_steps, true, false, stream());
+  else if (variant_ == kFusedTma)
+    err = tma::forward(a, second, &cur_, maps_, err_flag_.as<int>(), plans_[shot], shot, false, 0,
+                       n_steps, true, false, stream());
   else if (variant_ == kFused)
     err = fast::forward(a, second, &cur_, plans_[shot], shot, false, 0, n_steps, true, false,
                         stream());
@@ -502,11 +537,15 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
 }
 
 void Model::set_variant(int v) {
-  if (v != kFused && v != kTwoKernel) throw Error(PSV_ERR_INVALID_ARGUMENT, "unknown kernel variant");
-  if (prec_ == PSV_FP64 && v == kFused)
-    throw Error(PSV_ERR_INVALID_ARGUMENT, "the fused variant is FP32 only");
+  if (v != kFused && v != kTwoKernel && v != kFusedTma)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "unknown kernel variant");
+  if (prec_ == PSV_FP64 && v != kTwoKernel)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "the fused variants are FP32 only");
+  if (v == kFusedTma && !tma_ok_)
+    throw Error(PSV_ERR_INVALID_ARGUMENT,
+                "the TMA variant needs nz divisible by 4 (16-byte rows) and tensor-map support");
   DeviceGuard guard(device_);
-  if (v != variant_ && cur_ == 1) {
+  if ((v == kTwoKernel) != (variant_ == kTwoKernel) && cur_ == 1) {
     // Bring the current state back into the primary buffers.
     for (int f = 0; f < 5; ++f)
       cuda_check(cudaMemcpyAsync(fields_[f].get(), fields2_[f].get(), fields_[f].bytes(),
@@ -520,6 +559,7 @@ void Model::set_variant(int v) {
 
 const char *Model::step_kernel_name(int k) const {
   if (variant_ == kFused) return k == 0 ? "fused_step" : "";
+  if (variant_ == kFusedTma) return k == 0 ? "fused_step_tma" : "";
   return k == 0 ? "stress_step" : (k == 1 ? "velocity_step" : "");
 }
 
@@ -534,6 +574,9 @@ void Model::adjoint_simulate(int shot, bool verbose) {
   cudaError_t e;
   if (prec_ == PSV_FP64) {
     e = adjoint_f64(a, plans_[cfg_.n_shots], shot, stream());
+  } else if (variant_ == kFusedTma) {
+    e = tma::adjoint(a, second, &cur_, maps_, err_flag_.as<int>(), plans_[cfg_.n_shots], shot,
+                     stream());
   } else if (variant_ == kFused) {
     e = fast::adjoint(a, second, &cur_, plans_[cfg_.n_shots], shot, stream());
   } else {
@@ -542,6 +585,7 @@ void Model::adjoint_simulate(int shot, bool verbose) {
   }
   cuda_check(e, "adjoint_simulate");
   finish("adjoint_simulate");
+  if (!async_ && variant_ == kFusedTma) check_device_error();
   if (verbose) {
     synchronize();
     double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -11,6 +11,7 @@
 
 #include "psv_config.hpp"
 #include "psv_solver.hpp"
+#include "psv_tma.hpp"
 
 namespace psv {
 
@@ -115,7 +116,7 @@ class Model {
   // run kTwoKernel.
   void set_variant(int v);
   int variant() const { return variant_; }
-  int kernels_per_step() const { return variant_ == kFused ? 1 : 2; }
+  int kernels_per_step() const { return variant_ == kTwoKernel ? 2 : 1; }
   const char *step_kernel_name(int k) const;
 
   void set_stream(cudaStream_t s) { user_stream_ = s; }
@@ -154,7 +155,11 @@ class Model {
   std::vector<double> taper_tab_;                       // [np + 1]
 
   int variant_ = kTwoKernel;
-  int cur_ = 0;  // fused variant: 0 = fields_ hold the current state, 1 = fields2_
+  int cur_ = 0;  // fused variants: 0 = fields_ hold the current state, 1 = fields2_
+  bool tma_ok_ = false;   // TMA maps built for this model
+  tma::Maps maps_[2];     // tensor maps of fields_ (0) and fields2_ (1) + medium
+  void build_tma_maps();
+  void check_device_error();
 
   // Device arrays.
   DeviceBuffer fields_[5];                    // vx vz txx tzz txz   (T)
@@ -170,6 +175,7 @@ class Model {
   DeviceBuffer klame_[3];                     // lambda mu rho       (FP64)
   DeviceBuffer kvel_[3];                      // vp vs rho           (FP64)
   DeviceBuffer partials_, scalar_;            // reduction scratch   (FP64)
+  DeviceBuffer err_flag_;                     // int, raised by bounded device waits
   // Injection plans: one per shot (sources) and one for the adjoint receivers.
   std::vector<DeviceBuffer> plan_terms_, plan_maps_;
   std::vector<InjPlan> plans_;  // [n_shots] forward, [n_shots] = adjoint

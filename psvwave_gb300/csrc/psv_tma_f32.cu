@@ -1,0 +1,404 @@
+// FP32 fused time step with TMA tile loads (grids with nz % 4 == 0).
+//
+// Same step as psv_fast_f32.cu -- new stresses over the tile plus a 2-point
+// halo, then new velocities of the tile's own points, over ping-pong buffers
+// -- but the CTA's inputs arrive by tensor-memory-access bulk copies: thread 0
+// issues seven cp.async.bulk.tensor.2d loads (vx, vz with a 4-point halo;
+// txx, tzz, txz, lm, mu with a 2-point halo) that complete on one mbarrier,
+// and every phase then computes from shared memory. The copies zero-fill
+// whatever lies outside the grid. Stresses are advanced in place in shared
+// memory; lambda is lm - 2 mu.
+//
+// A TMA copy must start on a 16-byte boundary of the innermost (z) axis, so
+// every box starts at z = Z0 - 4 (Z0 a multiple of 64) and is 72 points wide;
+// the stress boxes use columns 2..69 of it.
+//
+// The mbarrier wait is bounded: on time-out the CTA raises the model's error
+// flag, waits (bounded again) for its copies to land, and returns.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "psv_fast.hpp"
+#include "psv_tma.hpp"
+
+namespace psv {
+namespace tma {
+namespace {
+
+constexpr int TX = 32, TZ = 64, NT = 256;
+constexpr int W = TZ + 8;          // box width (z) of every tile
+constexpr int VR = TX + 8;         // velocity box rows (x): X0-4 .. X0+TX+4
+constexpr int SR = TX + 4;         // stress / medium box rows: X0-2 .. X0+TX+2
+constexpr int kVBytes = VR * W * 4;  // 11520
+constexpr int kSBytes = SR * W * 4;  // 10368
+constexpr int kTxBytes = 2 * kVBytes + 5 * kSBytes;
+constexpr int kSmemBytes = kTxBytes + 16 + 128;  // tiles + mbarrier + alignment slack
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait on phase `parity`: true when the phase completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t max_iter) {
+  const uint32_t addr = smem_u32(bar);
+  for (uint32_t i = 0; i < max_iter; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity), "r"(1000u)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ float taper(const fast::StepArgs &a, int gx, int gz) {
+  int c = min(min(gx + 1, gz + 1), min(a.nx - gx, a.nz - gz));
+  return a.taper_tab[min(c, a.np)];
+}
+
+__device__ __forceinline__ void correlate(const fast::StepArgs &a, size_t g, float lm, float mu,
+                                          float vx, float vz, float txx, float tzz, float txz) {
+  const float la = lm - 2.0f * mu;
+  const float avx = a.asnap[0][g], avz = a.asnap[1][g], atxx = a.asnap[2][g],
+              atzz = a.asnap[3][g], atxz = a.asnap[4][g];
+  const float r = la / lm;
+  const float d = lm - la * r;
+  const float inv_den = 1.0f / (d * d);
+  const float fxx = txx - tzz * r, fzz = tzz - txx * r;
+  const float axx = atxx - atzz * r, azz = atzz - atxx * r;
+  const float lam = (axx + azz) * (fxx + fzz) * inv_den;
+  const float muk = (fxx * axx + fzz * azz) * inv_den + 2.0f * (txz * atxz / (4.0f * mu * mu));
+  a.krho[g] -= a.sidt * static_cast<double>(avx * vx + avz * vz);
+  a.klam[g] += a.sidt * static_cast<double>(lam);
+  a.kmu[g] += a.sidt * 2.0 * static_cast<double>(muk);
+}
+
+__device__ __forceinline__ void inject(const fast::StepArgs &a, size_t g, int gx, int gz,
+                                       float b, float &vx, float &vz) {
+  const InjPlan &p = a.plan;
+  int k = p.map[(gx - p.x0) * p.h + (gz - p.z0)];
+  if (k < 0) return;
+  for (; k < p.n && p.terms[k].cell == (int)g; ++k) {
+    const InjTerm t = p.terms[k];
+    double term;
+    if (t.kind == 0) {
+      term = (((t.coef * a.stf[(size_t)t.index * a.nt + a.it]) * a.dt_d) * (double)b) / t.div;
+    } else {
+      const double *src = t.field == 0 ? a.a_ux : a.a_uz;
+      term = ((a.dt_d * (double)b) * src[(size_t)t.index * a.nt + a.it]) / t.div;
+    }
+    if (t.field == 0)
+      vx += (float)term;
+    else
+      vz += (float)term;
+  }
+}
+
+template <bool ADJ>
+__global__ void __launch_bounds__(NT, 3)
+    fused_step_tma(const fast::StepArgs a, const __grid_constant__ Maps maps, int *err) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  float(*sv)[VR][W] = reinterpret_cast<float(*)[VR][W]>(base);                   // vx, vz
+  float(*st)[SR][W] = reinterpret_cast<float(*)[SR][W]>(base + 2 * kVBytes);    // txx tzz txz
+  float(*sm)[SR][W] = reinterpret_cast<float(*)[SR][W]>(base + 2 * kVBytes + 3 * kSBytes);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base + kTxBytes);
+
+  const int nx = a.nx, nz = a.nz;
+  const int X0 = blockIdx.y * TX, Z0 = blockIdx.x * TZ;
+  const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
+
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(1)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(kTxBytes)
+                 : "memory");
+    tma_load_2d(&sv[0][0][0], &maps.vx, Z0 - 4, X0 - 4, bar);
+    tma_load_2d(&sv[1][0][0], &maps.vz, Z0 - 4, X0 - 4, bar);
+    tma_load_2d(&st[0][0][0], &maps.txx, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&st[1][0][0], &maps.tzz, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&st[2][0][0], &maps.txz, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&sm[0][0][0], &maps.lm, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&sm[1][0][0], &maps.mu, Z0 - 4, X0 - 2, bar);
+  }
+
+  // While the copies fly: receivers (pre-step velocities) and this thread's
+  // buoyancy values for phase C.
+  if (!ADJ && a.rec_vx && blockIdx.x == 0 && blockIdx.y == 0) {
+    for (int r = threadIdx.x; r < a.nr; r += NT) {
+      const int c = a.rec_cell[r];
+      a.rec_vx[(size_t)r * a.nt + a.it] = a.in.vx[c];
+      a.rec_vz[(size_t)r * a.nt + a.it] = a.in.vz[c];
+    }
+  }
+  constexpr int KC = TX * TZ / NT;
+  float bb[KC];
+#pragma unroll
+  for (int k = 0; k < KC; ++k) {
+    const int e = threadIdx.x + k * NT;
+    const int gx = X0 + e / TZ, gz = Z0 + e % TZ;
+    bb[k] = (gx < nx && gz < nz) ? __ldg(a.b + (size_t)gx * nz + gz) : 0.f;
+  }
+
+  // Bounded wait (about a second at most); the CTA agrees on the outcome so
+  // that it leaves together, after its copies have landed.
+  const bool landed = mbar_wait(bar, 0, 1u << 20);
+  if (__syncthreads_or(!landed)) {
+    if (threadIdx.x == 0) {
+      atomicOr(err, 1);
+      mbar_wait(bar, 0, 1u << 20);
+    }
+    return;
+  }
+
+  // Phase B: new stresses over rows X0-2 .. X0+TX+2, columns Z0-2 .. Z0+TZ+2
+  // (box columns 2 .. TZ+6), in place.
+  {
+    const float(*VX)[W] = sv[0];
+    const float(*VZ)[W] = sv[1];
+    constexpr int NC = TZ + 4, N = SR * NC;
+    for (int e = threadIdx.x; e < N; e += NT) {
+      const int r = e / NC, c = e - r * NC + 2;  // box row, box column
+      const int gx = X0 - 2 + r, gz = Z0 - 4 + c;
+      if (gx < 0 || gx >= nx || gz < 0 || gz >= nz) continue;
+      const size_t g = (size_t)gx * nz + gz;
+      const int vr = r + 2;  // same point in the velocity box
+      float sxx = st[0][r][c], szz = st[1][r][c], sxz = st[2][r][c];
+      const bool own = r >= 2 && r < TX + 2 && c >= 4 && c < TZ + 4;
+      if (own && a.snap[0]) {
+        a.snap[0][g] = VX[vr][c];
+        a.snap[1][g] = VZ[vr][c];
+        a.snap[2][g] = sxx;
+        a.snap[3][g] = szz;
+        a.snap[4][g] = sxz;
+      }
+      const float lm = sm[0][r][c], mu = sm[1][r][c];
+      if (ADJ && own && a.asnap[0] && gx >= a.fx0 && gx < a.fx1 && gz >= a.fz0 && gz < a.fz1)
+        correlate(a, g, lm, mu, VX[vr][c], VZ[vr][c], sxx, szz, sxz);
+      if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
+        const float la = lm - 2.0f * mu;
+        const float dvx = c1 * (VX[vr + 1][c] - VX[vr][c]) + c2 * (VX[vr - 1][c] - VX[vr + 2][c]);
+        const float dvz = c1 * (VZ[vr][c] - VZ[vr][c - 1]) + c2 * (VZ[vr][c - 2] - VZ[vr][c + 1]);
+        const float gxz = (c1 * (VX[vr][c + 1] - VX[vr][c]) +
+                           c2 * (VX[vr][c - 1] - VX[vr][c + 2])) * a.idz +
+                          (c1 * (VZ[vr][c] - VZ[vr - 1][c]) +
+                           c2 * (VZ[vr - 2][c] - VZ[vr + 1][c])) * a.idx;
+        const float ex = dvx * a.idx, ez = dvz * a.idz;
+        const float tp = taper(a, gx, gz);
+        const float dt = ADJ ? -a.dt : a.dt;
+        sxx = tp * (sxx + dt * (lm * ex + la * ez));
+        szz = tp * (szz + dt * (la * ex + lm * ez));
+        sxz = tp * (sxz + dt * mu * gxz);
+        st[0][r][c] = sxx;
+        st[1][r][c] = szz;
+        st[2][r][c] = sxz;
+      }
+      if (own) {
+        a.out.txx[g] = sxx;
+        a.out.tzz[g] = szz;
+        a.out.txz[g] = sxz;
+      }
+    }
+  }
+  __syncthreads();
+
+  // Phase C: new velocities of the tile's own points.
+  {
+    const float(*TXX)[W] = st[0];
+    const float(*TZZ)[W] = st[1];
+    const float(*TXZ)[W] = st[2];
+    const InjPlan &p = a.plan;
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+      const int e = threadIdx.x + k * NT;
+      const int lx = e / TZ, lz = e % TZ;
+      const int gx = X0 + lx, gz = Z0 + lz;
+      if (gx >= nx || gz >= nz) continue;
+      const size_t g = (size_t)gx * nz + gz;
+      const int r = lx + 2, c = lz + 4;  // stress box coordinates of this point
+      float vx = sv[0][lx + 4][c], vz = sv[1][lx + 4][c];
+      const float b = bb[k];
+      if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
+        const float ax = (c1 * (TXX[r][c] - TXX[r - 1][c]) + c2 * (TXX[r - 2][c] - TXX[r + 1][c])) * a.idx +
+                         (c1 * (TXZ[r][c] - TXZ[r][c - 1]) + c2 * (TXZ[r][c - 2] - TXZ[r][c + 1])) * a.idz;
+        const float az = (c1 * (TXZ[r + 1][c] - TXZ[r][c]) + c2 * (TXZ[r - 1][c] - TXZ[r + 2][c])) * a.idx +
+                         (c1 * (TZZ[r][c + 1] - TZZ[r][c]) + c2 * (TZZ[r][c - 1] - TZZ[r][c + 2])) * a.idz;
+        const float tp = taper(a, gx, gz);
+        const float bdt = b * (ADJ ? -a.dt : a.dt);
+        vx = tp * (vx + bdt * ax);
+        vz = tp * (vz + bdt * az);
+      }
+      if (p.n && gx >= p.x0 && gx < p.x0 + p.w && gz >= p.z0 && gz < p.z0 + p.h)
+        inject(a, g, gx, gz, b, vx, vz);
+      a.out.vx[g] = vx;
+      a.out.vz[g] = vz;
+    }
+  }
+}
+
+template <bool ADJ>
+cudaError_t launch(const fast::StepArgs &a, const Maps &maps, int *err, cudaStream_t s) {
+  static unsigned long long configured = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(configured & bit)) {
+    e = cudaFuncSetAttribute(fused_step_tma<ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kSmemBytes);
+    if (e != cudaSuccess) return e;
+    configured |= bit;
+  }
+  const dim3 grid((a.nz + TZ - 1) / TZ, (a.nx + TX - 1) / TX);
+  fused_step_tma<ADJ><<<grid, NT, kSmemBytes, s>>>(a, maps, err);
+  return cudaGetLastError();
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                 const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                 const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+  static EncodeTiled fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  }
+  return fn;
+}
+
+bool encode(CUtensorMap *m, const float *ptr, int nx, int nz, int rows) {
+  EncodeTiled fn = encoder();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)nz, (cuuint64_t)nx};
+  const cuuint64_t strides[1] = {(cuuint64_t)nz * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)rows};
+  const cuuint32_t elem[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(ptr), dims, strides, box,
+            elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+}  // namespace
+
+bool supported(int nx, int nz) { return nz % 4 == 0 && nx > 0 && nz > 0 && encoder() != nullptr; }
+
+bool make_maps(Maps &m, const float *const fields[5], const float *lm, const float *mu, int nx,
+               int nz) {
+  return encode(&m.vx, fields[0], nx, nz, VR) && encode(&m.vz, fields[1], nx, nz, VR) &&
+         encode(&m.txx, fields[2], nx, nz, SR) && encode(&m.tzz, fields[3], nx, nz, SR) &&
+         encode(&m.txz, fields[4], nx, nz, SR) && encode(&m.lm, lm, nx, nz, SR) &&
+         encode(&m.mu, mu, nx, nz, SR);
+}
+
+cudaError_t forward(const SolverArgs &a, void *const second[5], int *cur, const Maps maps[2],
+                    int *err, const InjPlan &plan, int shot, bool store, int it0, int it1,
+                    bool zero_first, bool finish, cudaStream_t s) {
+  if (zero_first) {
+    const size_t bytes = (size_t)a.nx * a.nz * sizeof(float);
+    void *prim[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
+    for (int f = 0; f < 5; ++f) {
+      cudaError_t e = cudaMemsetAsync(prim[f], 0, bytes, s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(second[f], 0, bytes, s);
+      if (e != cudaSuccess) return e;
+    }
+    *cur = 0;
+  }
+  fast::StepArgs sa = fast::base_step_args(a);
+  sa.plan = plan;
+  sa.stf = a.stf;
+  sa.rec_cell = a.rec_cell;
+  sa.nr = a.nr;
+  float *raw = (float *)a.rec_raw;
+  sa.rec_vx = a.nr ? raw : nullptr;
+  sa.rec_vz = a.nr ? raw + (size_t)a.nr * a.nt : nullptr;
+  const size_t gsz = (size_t)a.nx * a.nz;
+  for (int it = it0; it < it1; ++it) {
+    sa.it = it;
+    for (int f = 0; f < 5; ++f)
+      sa.snap[f] = (store && it % a.si == 0)
+                       ? (float *)a.accu[f] + ((size_t)shot * a.snapshots + it / a.si) * gsz
+                       : nullptr;
+    fast::set_step_buffers(sa, a, second, *cur);
+    cudaEvent_t *ev = a.events ? a.events + 2 * (it - it0) : nullptr;
+    if (ev) cudaEventRecord(ev[0], s);
+    cudaError_t e = launch<false>(sa, maps[*cur], err, s);
+    if (ev) cudaEventRecord(ev[1], s);
+    if (e != cudaSuccess) return e;
+    *cur ^= 1;
+  }
+  if (finish && a.nr) {
+    const size_t off = (size_t)shot * a.nr * a.nt;
+    receiver_cumsum_f32(a.nr, a.nt, it1, a.dt, a.dx * a.dz, sa.rec_vx, sa.rec_vz,
+                        a.rtf_ux + off, a.rtf_uz + off, s);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t adjoint(const SolverArgs &a, void *const second[5], int *cur, const Maps maps[2],
+                    int *err, const InjPlan &plan, int shot, cudaStream_t s) {
+  const size_t bytes = (size_t)a.nx * a.nz * sizeof(float);
+  void *prim[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
+  for (int f = 0; f < 5; ++f) {
+    cudaError_t e = cudaMemsetAsync(prim[f], 0, bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(second[f], 0, bytes, s);
+    if (e != cudaSuccess) return e;
+  }
+  *cur = 0;
+  fast::StepArgs sa = fast::base_step_args(a);
+  sa.plan = plan;
+  sa.a_ux = a.a_stf_ux + (size_t)shot * a.nr * a.nt;
+  sa.a_uz = a.a_stf_uz + (size_t)shot * a.nr * a.nt;
+  sa.krho = a.k_rho;
+  sa.klam = a.k_lam;
+  sa.kmu = a.k_mu;
+  sa.sidt = a.si * a.dt;
+  sa.fx0 = a.fx0;
+  sa.fx1 = a.fx1;
+  sa.fz0 = a.fz0;
+  sa.fz1 = a.fz1;
+  const size_t gsz = (size_t)a.nx * a.nz;
+  for (int it = a.nt - 1; it >= 0; --it) {
+    sa.it = it;
+    for (int f = 0; f < 5; ++f)
+      sa.asnap[f] = (it % a.si == 0)
+                        ? (const float *)a.accu[f] + ((size_t)shot * a.snapshots + it / a.si) * gsz
+                        : nullptr;
+    fast::set_step_buffers(sa, a, second, *cur);
+    cudaError_t e = launch<true>(sa, maps[*cur], err, s);
+    if (e != cudaSuccess) return e;
+    *cur ^= 1;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tma
+}  // namespace psv

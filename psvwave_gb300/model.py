@@ -410,15 +410,16 @@ class fdModel:
         names = [self._lib.psv_step_kernel_name(self._h, k).decode() for k in range(n.value)]
         return per_step.value, dict(zip(names, list(ks)[:n.value]))
 
-    VARIANTS = {"fused": 0, "two_kernel": 1}
+    VARIANTS = {"fused": 0, "two_kernel": 1, "fused_tma": 2}
 
     @property
     def kernel_variant(self):
-        """'fused' (one launch per step, FP32) or 'two_kernel' (stress and
-        velocity launches; the FP64 variant)."""
+        """'fused_tma' (one launch per step with TMA tile loads; FP32 grids
+        with nz % 4 == 0), 'fused' (one launch per step, FP32) or
+        'two_kernel' (stress and velocity launches; the FP64 variant)."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_get_kernel_variant(self._h, ctypes.byref(v)))
-        return {0: "fused", 1: "two_kernel"}[v.value]
+        return {0: "fused", 1: "two_kernel", 2: "fused_tma"}[v.value]
 
     @kernel_variant.setter
     def kernel_variant(self, name):

@@ -155,7 +155,15 @@ def test_fp32_vs_fp64_gpu_nb2_full_outputs():
         assert e <= FP32_TOL, (k, e)
 
 
-@pytest.mark.parametrize("variant", ["fused", "two_kernel"])
+def test_default_fp32_variant_depends_on_row_alignment():
+    assert psv.fdModel(SMALL_INI).kernel_variant == "fused_tma"   # nz = 56
+    assert psv.fdModel(NB2_INI).kernel_variant == "fused"         # nz = 150
+    assert psv.fdModel(SMALL_INI, precision="fp64").kernel_variant == "two_kernel"
+    with pytest.raises(ValueError):
+        psv.fdModel(NB2_INI).kernel_variant = "fused_tma"
+
+
+@pytest.mark.parametrize("variant", ["fused_tma", "fused", "two_kernel"])
 def test_fp32_variants_within_tolerance(golden, variant):
     m = psv.fdModel(SMALL_INI, precision="fp32")
     m.kernel_variant = variant
@@ -189,3 +197,20 @@ def test_fp64_rejects_fused_variant():
     m = psv.fdModel(SMALL_INI, precision="fp64")
     with pytest.raises(ValueError):
         m.kernel_variant = "fused"
+
+
+def test_fp32_tma_vs_two_kernel_agree(golden):
+    """The TMA variant against the two-kernel variant on the small grid:
+    seismograms and every stored snapshot agree to FP32 rounding."""
+    res = []
+    for variant in ("fused_tma", "two_kernel"):
+        m = psv.fdModel(SMALL_INI, precision="fp32")
+        m.kernel_variant = variant
+        m.set_parameter_fields(*golden["target"])
+        for s in range(m.n_shots):
+            m.forward_simulate(s, True)
+        res.append((m.get_synthetic_data(), m.get_snapshots()))
+    for a, b in zip(res[0][0], res[1][0]):
+        assert rel_l2(a, b) <= 1e-5
+    for a, b in zip(res[0][1], res[1][1]):
+        assert rel_l2(a, b) <= 1e-5
