@@ -10,8 +10,10 @@
 // memory; lambda is lm - 2 mu.
 //
 // A TMA copy must start on a 16-byte boundary of the innermost (z) axis, so
-// every box starts at z = Z0 - 4 (Z0 a multiple of 64) and is 72 points wide;
-// the stress boxes use columns 2..69 of it.
+// every box starts at z = Z0 - 4 (Z0 a multiple of 60, so 4 (Z0 - 4) is a
+// multiple of 16) and is 68 points wide; the stress boxes use columns 2..65.
+// Each warp of the compute phases owns 32 consecutive z columns and walks
+// every fourth row, so column arithmetic is done once per thread.
 //
 // The mbarrier wait is bounded: on time-out the CTA raises the model's error
 // flag, waits (bounded again) for its copies to land, and returns.
@@ -27,14 +29,19 @@ namespace psv {
 namespace tma {
 namespace {
 
-constexpr int TX = 32, TZ = 64, NT = 256;
-constexpr int W = TZ + 8;          // box width (z) of every tile
+constexpr int TX = 32, TZ = 60, NT = 256;
+constexpr int W = TZ + 8;          // box width (z) of every tile: Z0-4 .. Z0+TZ+4
 constexpr int VR = TX + 8;         // velocity box rows (x): X0-4 .. X0+TX+4
 constexpr int SR = TX + 4;         // stress / medium box rows: X0-2 .. X0+TX+2
-constexpr int kVBytes = VR * W * 4;  // 11520
-constexpr int kSBytes = SR * W * 4;  // 10368
-constexpr int kTxBytes = 2 * kVBytes + 5 * kSBytes;
-constexpr int kSmemBytes = kTxBytes + 16 + 128;  // tiles + mbarrier + alignment slack
+constexpr int SC = TZ + 4;         // stress columns computed: box columns 2 .. TZ+6
+constexpr int kVBytes = VR * W * 4;                      // 10880
+constexpr int kSBytes = SR * W * 4;                      // 9792
+constexpr int kSPitch = (kSBytes + 127) / 128 * 128;     // 128-byte aligned tile slots
+constexpr int kTxBytes = 2 * kVBytes + 5 * kSBytes;      // bytes the copies deliver
+constexpr int kTileBytes = 2 * kVBytes + 5 * kSPitch;
+constexpr int kSmemBytes = kTileBytes + 16 + 128;        // tiles + mbarrier + alignment slack
+static_assert(kVBytes % 128 == 0, "velocity tiles must stay 128-byte aligned");
+static_assert(SC == 64, "two warps span the stress columns");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -64,11 +71,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
     if (done) return true;
   }
   return false;
-}
-
-__device__ __forceinline__ float taper(const fast::StepArgs &a, int gx, int gz) {
-  int c = min(min(gx + 1, gz + 1), min(a.nx - gx, a.nz - gz));
-  return a.taper_tab[min(c, a.np)];
 }
 
 __device__ __forceinline__ void correlate(const fast::StepArgs &a, size_t g, float lm, float mu,
@@ -115,10 +117,16 @@ __global__ void __launch_bounds__(NT, 3)
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
-  float(*sv)[VR][W] = reinterpret_cast<float(*)[VR][W]>(base);                   // vx, vz
-  float(*st)[SR][W] = reinterpret_cast<float(*)[SR][W]>(base + 2 * kVBytes);    // txx tzz txz
-  float(*sm)[SR][W] = reinterpret_cast<float(*)[SR][W]>(base + 2 * kVBytes + 3 * kSBytes);
-  uint64_t *bar = reinterpret_cast<uint64_t *>(base + kTxBytes);
+  float(*sv)[VR][W] = reinterpret_cast<float(*)[VR][W]>(base);  // vx, vz
+  auto stile = [&](int k) {  // txx tzz txz lm mu
+    return reinterpret_cast<float(*)[W]>(base + 2 * kVBytes + k * kSPitch);
+  };
+  float(*const sxx_)[W] = stile(0);
+  float(*const szz_)[W] = stile(1);
+  float(*const sxz_)[W] = stile(2);
+  float(*const slm)[W] = stile(3);
+  float(*const smu)[W] = stile(4);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base + kTileBytes);
 
   const int nx = a.nx, nz = a.nz;
   const int X0 = blockIdx.y * TX, Z0 = blockIdx.x * TZ;
@@ -137,11 +145,11 @@ __global__ void __launch_bounds__(NT, 3)
                  : "memory");
     tma_load_2d(&sv[0][0][0], &maps.vx, Z0 - 4, X0 - 4, bar);
     tma_load_2d(&sv[1][0][0], &maps.vz, Z0 - 4, X0 - 4, bar);
-    tma_load_2d(&st[0][0][0], &maps.txx, Z0 - 4, X0 - 2, bar);
-    tma_load_2d(&st[1][0][0], &maps.tzz, Z0 - 4, X0 - 2, bar);
-    tma_load_2d(&st[2][0][0], &maps.txz, Z0 - 4, X0 - 2, bar);
-    tma_load_2d(&sm[0][0][0], &maps.lm, Z0 - 4, X0 - 2, bar);
-    tma_load_2d(&sm[1][0][0], &maps.mu, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&sxx_[0][0], &maps.txx, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&szz_[0][0], &maps.tzz, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&sxz_[0][0], &maps.txz, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&slm[0][0], &maps.lm, Z0 - 4, X0 - 2, bar);
+    tma_load_2d(&smu[0][0], &maps.mu, Z0 - 4, X0 - 2, bar);
   }
 
   // While the copies fly: receivers (pre-step velocities) and this thread's
@@ -153,13 +161,18 @@ __global__ void __launch_bounds__(NT, 3)
       a.rec_vz[(size_t)r * a.nt + a.it] = a.in.vz[c];
     }
   }
-  constexpr int KC = TX * TZ / NT;
+  // Thread layout for both compute phases: warp w covers 32 consecutive z
+  // columns (half h = w & 1 of the tile) and every fourth row from q = w >> 1.
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = w & 1, q = w >> 1;
+  constexpr int KC = TX / 4;  // own rows per thread
+  const int lzc = h * 32 + lane;  // own column of this thread (valid if < TZ)
+  const int gzc = Z0 + lzc;
+  const bool col_ok = lzc < TZ && gzc < nz;
   float bb[KC];
 #pragma unroll
   for (int k = 0; k < KC; ++k) {
-    const int e = threadIdx.x + k * NT;
-    const int gx = X0 + e / TZ, gz = Z0 + e % TZ;
-    bb[k] = (gx < nx && gz < nz) ? __ldg(a.b + (size_t)gx * nz + gz) : 0.f;
+    const int gx = X0 + q + 4 * k;
+    bb[k] = (col_ok && gx < nx) ? __ldg(a.b + gx * nz + gzc) : 0.f;
   }
 
   // Bounded wait (about a second at most); the CTA agrees on the outcome so
@@ -173,20 +186,28 @@ __global__ void __launch_bounds__(NT, 3)
     return;
   }
 
-  // Phase B: new stresses over rows X0-2 .. X0+TX+2, columns Z0-2 .. Z0+TZ+2
-  // (box columns 2 .. TZ+6), in place.
+  const float dtv = ADJ ? -a.dt : a.dt;
+  // Phase B: new stresses over rows X0-2 .. X0+TX+2 and box columns
+  // 2 .. TZ+6 (z = Z0-2 .. Z0+TZ+2), in place.
   {
     const float(*VX)[W] = sv[0];
     const float(*VZ)[W] = sv[1];
-    constexpr int NC = TZ + 4, N = SR * NC;
-    for (int e = threadIdx.x; e < N; e += NT) {
-      const int r = e / NC, c = e - r * NC + 2;  // box row, box column
-      const int gx = X0 - 2 + r, gz = Z0 - 4 + c;
-      if (gx < 0 || gx >= nx || gz < 0 || gz >= nz) continue;
-      const size_t g = (size_t)gx * nz + gz;
+    const int c = 2 + h * 32 + lane;  // box column
+    const int gz = Z0 - 4 + c;
+    const bool z_in = gz >= 0 && gz < nz;
+    const bool z_int = gz >= 2 && gz < nz - 2;
+    const bool z_own = c >= 4 && c < TZ + 4;
+    const bool z_free = gz >= a.fz0 && gz < a.fz1;
+    const int tz = min(gz + 1, nz - gz);
+#pragma unroll 3
+    for (int k = 0; k < SR / 4; ++k) {
+      const int r = q + 4 * k;  // box row
+      const int gx = X0 - 2 + r;
+      if (!z_in || gx < 0 || gx >= nx) continue;
+      const int g = gx * nz + gz;
       const int vr = r + 2;  // same point in the velocity box
-      float sxx = st[0][r][c], szz = st[1][r][c], sxz = st[2][r][c];
-      const bool own = r >= 2 && r < TX + 2 && c >= 4 && c < TZ + 4;
+      float sxx = sxx_[r][c], szz = szz_[r][c], sxz = sxz_[r][c];
+      const bool own = z_own && r >= 2 && r < TX + 2;
       if (own && a.snap[0]) {
         a.snap[0][g] = VX[vr][c];
         a.snap[1][g] = VZ[vr][c];
@@ -194,10 +215,10 @@ __global__ void __launch_bounds__(NT, 3)
         a.snap[3][g] = szz;
         a.snap[4][g] = sxz;
       }
-      const float lm = sm[0][r][c], mu = sm[1][r][c];
-      if (ADJ && own && a.asnap[0] && gx >= a.fx0 && gx < a.fx1 && gz >= a.fz0 && gz < a.fz1)
+      const float lm = slm[r][c], mu = smu[r][c];
+      if (ADJ && own && a.asnap[0] && z_free && gx >= a.fx0 && gx < a.fx1)
         correlate(a, g, lm, mu, VX[vr][c], VZ[vr][c], sxx, szz, sxz);
-      if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
+      if (z_int && gx >= 2 && gx < nx - 2) {
         const float la = lm - 2.0f * mu;
         const float dvx = c1 * (VX[vr + 1][c] - VX[vr][c]) + c2 * (VX[vr - 1][c] - VX[vr + 2][c]);
         const float dvz = c1 * (VZ[vr][c] - VZ[vr][c - 1]) + c2 * (VZ[vr][c - 2] - VZ[vr][c + 1]);
@@ -206,14 +227,14 @@ __global__ void __launch_bounds__(NT, 3)
                           (c1 * (VZ[vr][c] - VZ[vr - 1][c]) +
                            c2 * (VZ[vr - 2][c] - VZ[vr + 1][c])) * a.idx;
         const float ex = dvx * a.idx, ez = dvz * a.idz;
-        const float tp = taper(a, gx, gz);
-        const float dt = ADJ ? -a.dt : a.dt;
-        sxx = tp * (sxx + dt * (lm * ex + la * ez));
-        szz = tp * (szz + dt * (la * ex + lm * ez));
-        sxz = tp * (sxz + dt * mu * gxz);
-        st[0][r][c] = sxx;
-        st[1][r][c] = szz;
-        st[2][r][c] = sxz;
+        const int cnt = min(min(tz, min(gx + 1, nx - gx)), a.np);
+        const float tp = a.taper_tab[cnt];
+        sxx = tp * (sxx + dtv * (lm * ex + la * ez));
+        szz = tp * (szz + dtv * (la * ex + lm * ez));
+        sxz = tp * (sxz + dtv * mu * gxz);
+        sxx_[r][c] = sxx;
+        szz_[r][c] = szz;
+        sxz_[r][c] = sxz;
       }
       if (own) {
         a.out.txx[g] = sxx;
@@ -225,33 +246,36 @@ __global__ void __launch_bounds__(NT, 3)
   __syncthreads();
 
   // Phase C: new velocities of the tile's own points.
-  {
-    const float(*TXX)[W] = st[0];
-    const float(*TZZ)[W] = st[1];
-    const float(*TXZ)[W] = st[2];
+  if (col_ok) {
+    const float(*TXX)[W] = sxx_;
+    const float(*TZZ)[W] = szz_;
+    const float(*TXZ)[W] = sxz_;
     const InjPlan &p = a.plan;
+    const int c = lzc + 4;  // box column of this thread's points
+    const bool z_int = gzc >= 2 && gzc < nz - 2;
+    const int tz = min(gzc + 1, nz - gzc);
+    const bool z_box = p.n && gzc >= p.z0 && gzc < p.z0 + p.h;
 #pragma unroll
     for (int k = 0; k < KC; ++k) {
-      const int e = threadIdx.x + k * NT;
-      const int lx = e / TZ, lz = e % TZ;
-      const int gx = X0 + lx, gz = Z0 + lz;
-      if (gx >= nx || gz >= nz) continue;
-      const size_t g = (size_t)gx * nz + gz;
-      const int r = lx + 2, c = lz + 4;  // stress box coordinates of this point
+      const int lx = q + 4 * k;
+      const int gx = X0 + lx;
+      if (gx >= nx) continue;
+      const int g = gx * nz + gzc;
+      const int r = lx + 2;  // stress box row
       float vx = sv[0][lx + 4][c], vz = sv[1][lx + 4][c];
       const float b = bb[k];
-      if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
+      if (z_int && gx >= 2 && gx < nx - 2) {
         const float ax = (c1 * (TXX[r][c] - TXX[r - 1][c]) + c2 * (TXX[r - 2][c] - TXX[r + 1][c])) * a.idx +
                          (c1 * (TXZ[r][c] - TXZ[r][c - 1]) + c2 * (TXZ[r][c - 2] - TXZ[r][c + 1])) * a.idz;
         const float az = (c1 * (TXZ[r + 1][c] - TXZ[r][c]) + c2 * (TXZ[r - 1][c] - TXZ[r + 2][c])) * a.idx +
                          (c1 * (TZZ[r][c + 1] - TZZ[r][c]) + c2 * (TZZ[r][c - 1] - TZZ[r][c + 2])) * a.idz;
-        const float tp = taper(a, gx, gz);
-        const float bdt = b * (ADJ ? -a.dt : a.dt);
+        const int cnt = min(min(tz, min(gx + 1, nx - gx)), a.np);
+        const float tp = a.taper_tab[cnt];
+        const float bdt = b * dtv;
         vx = tp * (vx + bdt * ax);
         vz = tp * (vz + bdt * az);
       }
-      if (p.n && gx >= p.x0 && gx < p.x0 + p.w && gz >= p.z0 && gz < p.z0 + p.h)
-        inject(a, g, gx, gz, b, vx, vz);
+      if (z_box && gx >= p.x0 && gx < p.x0 + p.w) inject(a, g, gx, gzc, b, vx, vz);
       a.out.vx[g] = vx;
       a.out.vz[g] = vz;
     }
