@@ -206,6 +206,10 @@ int psv_set_stream(psv_model *m, void *stream);
 /* Make forward/adjoint return without waiting for the GPU (1) or wait, as
  * the reference's calls do (0, the default). */
 int psv_set_async(psv_model *m, int async_calls);
+/* Replay repeated forward/adjoint time loops as CUDA graphs (1, the
+ * default: a loop is captured on its second identical call) or always launch
+ * kernel by kernel (0). No counterpart in the reference. */
+int psv_set_graph_capture(psv_model *m, int enable);
 int psv_synchronize(psv_model *m);
 /* Parameter fields from device FP64 buffers [nx][nz]. */
 int psv_set_parameter_fields_device(psv_model *m, const double *vp, const double *vs,
@@ -234,7 +238,7 @@ const char *psv_step_kernel_name(const psv_model *m, int k);
  * ping-pong buffers; FP32 only, the FP32 default) or PSV_VARIANT_TWO_KERNEL
  * (separate stress and velocity launches, as the reference's two loop nests;
  * the only FP64 variant) or PSV_VARIANT_FUSED_TMA (the fused step with TMA
- * tile loads; FP32 grids with nz % 4 == 0, where it is the default). Results
+ * tile loads; FP32, the default). Results
  * of the FP32 variants agree to FP32 rounding. No counterpart in the
  * reference. */
 enum psv_variant { PSV_VARIANT_FUSED = 0, PSV_VARIANT_TWO_KERNEL = 1, PSV_VARIANT_FUSED_TMA = 2 };

@@ -102,6 +102,7 @@ _SIGNATURES = {
     "psv_write_kernels": [_vp],
     "psv_set_stream": [_vp, _vp],
     "psv_set_async": [_vp, _c_int],
+    "psv_set_graph_capture": [_vp, _c_int],
     "psv_synchronize": [_vp],
     "psv_set_parameter_fields_device": [_vp, _vp, _vp, _vp],
     "psv_set_observed_data_device": [_vp, _vp, _vp],

@@ -462,6 +462,10 @@ int psv_set_async(psv_model *m, int async_calls) {
   return guarded([&] { M(m).set_async(async_calls != 0); });
 }
 
+int psv_set_graph_capture(psv_model *m, int enable) {
+  return guarded([&] { M(m).set_graphs(enable != 0); });
+}
+
 int psv_synchronize(psv_model *m) {
   return guarded([&] { M(m).synchronize(); });
 }

@@ -17,6 +17,7 @@ struct ConstFields {
 
 struct StepArgs {
   int nx = 0, nz = 0, np = 0, nt = 0, it = 0;
+  int pitch = 0;  // row pitch of wave-field and medium arrays
   float dt = 0, idx = 0, idz = 0;  // time step, 1/dx, 1/dz
   double dt_d = 0;
   ConstFields in{};

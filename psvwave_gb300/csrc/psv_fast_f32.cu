@@ -32,13 +32,14 @@ constexpr int SXD = TX + 4, SZD = TZ + 4;  // new-stress tile with 2-point halo
 constexpr int kSmemBytes = (2 * VXD * VZD + 3 * SXD * SZD) * 4;
 
 __device__ __forceinline__ float taper(const StepArgs &a, int gx, int gz) {
+  // Points at least np frames deep have taper exp(0) = 1 exactly.
   int c = min(min(gx + 1, gz + 1), min(a.nx - gx, a.nz - gz));
-  return a.taper_tab[min(c, a.np)];
+  return c < a.np ? __ldg(a.taper_tab + c) : 1.0f;
 }
 
-__device__ __forceinline__ void correlate(const StepArgs &a, size_t g, float vx, float vz,
-                                          float txx, float tzz, float txz) {
-  const float lm = a.lm[g], la = a.la[g], mu = a.mu[g];
+__device__ __forceinline__ void correlate(const StepArgs &a, size_t g, size_t gp, float vx,
+                                          float vz, float txx, float tzz, float txz) {
+  const float lm = a.lm[gp], la = a.la[gp], mu = a.mu[gp];
   const float avx = a.asnap[0][g], avz = a.asnap[1][g], atxx = a.asnap[2][g],
               atzz = a.asnap[3][g], atxz = a.asnap[4][g];
   const float r = la / lm;
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
   extern __shared__ float smem[];
   float(*sv)[VXD][VZD] = reinterpret_cast<float(*)[VXD][VZD]>(smem);
   float(*st)[SXD][SZD] = reinterpret_cast<float(*)[SXD][SZD]>(smem + 2 * VXD * VZD);
-  const int nx = a.nx, nz = a.nz;
+  const int nx = a.nx, nz = a.nz, ps = a.pitch;
   const int X0 = blockIdx.y * TX, Z0 = blockIdx.x * TZ;
   const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
 
@@ -106,7 +107,7 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
       rx[k] = 0.f;
       rz[k] = 0.f;
       if (e < N && gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
-        const size_t g = (size_t)gx * nz + gz;
+        const size_t g = (size_t)gx * ps + gz;
         rx[k] = __ldg(a.in.vx + g);
         rz[k] = __ldg(a.in.vz + g);
       }
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
         txx[j] = tzz[j] = txz[j] = 0.f;
         lm[j] = la[j] = mu[j] = 0.f;
         if (k0 + j < K && e < N && gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
-          const size_t g = (size_t)gx * nz + gz;
+          const size_t g = (size_t)gx * ps + gz;
           txx[j] = __ldg(a.in.txx + g);
           tzz[j] = __ldg(a.in.tzz + g);
           txz[j] = __ldg(a.in.txz + g);
@@ -157,7 +158,8 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
         const int gx = X0 - 2 + lx, gz = Z0 - 2 + lz;
         float sxx = txx[j], szz = tzz[j], sxz = txz[j];
         if (gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
-          const size_t g = (size_t)gx * nz + gz;
+          const size_t g = (size_t)gx * nz + gz;   // unpadded (snapshots, kernels)
+          const size_t gp = (size_t)gx * ps + gz;  // padded (wave fields, medium)
           const bool own = lx >= 2 && lx < TX + 2 && lz >= 2 && lz < TZ + 2;
           const int vx_ = lx + 2, vz_ = lz + 2;  // this point in the velocity tile
           if (own && a.snap[0]) {
@@ -169,7 +171,7 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
           }
           if (ADJ && own && a.asnap[0] && gx >= a.fx0 && gx < a.fx1 && gz >= a.fz0 &&
               gz < a.fz1)
-            correlate(a, g, VX[vx_][vz_], VZ[vx_][vz_], sxx, szz, sxz);
+            correlate(a, g, gp, VX[vx_][vz_], VZ[vx_][vz_], sxx, szz, sxz);
           if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
             const float dvx = c1 * (VX[vx_ + 1][vz_] - VX[vx_][vz_]) +
                               c2 * (VX[vx_ - 1][vz_] - VX[vx_ + 2][vz_]);
@@ -187,9 +189,9 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
             sxz = tp * (sxz + dt * mu[j] * gxz);
           }
           if (own) {
-            a.out.txx[g] = sxx;
-            a.out.tzz[g] = szz;
-            a.out.txz[g] = sxz;
+            a.out.txx[gp] = sxx;
+            a.out.tzz[gp] = szz;
+            a.out.txz[gp] = sxz;
           }
         }
         st[0][lx][lz] = sxx;
@@ -212,7 +214,7 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
     for (int k = 0; k < K; ++k) {
       const int e = threadIdx.x + k * NT;
       const int gx = X0 + e / TZ, gz = Z0 + e % TZ;
-      bb[k] = (gx < nx && gz < nz) ? __ldg(a.b + (size_t)gx * nz + gz) : 0.f;
+      bb[k] = (gx < nx && gz < nz) ? __ldg(a.b + (size_t)gx * ps + gz) : 0.f;
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -220,7 +222,8 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
       const int lx = e / TZ, lz = e % TZ;
       const int gx = X0 + lx, gz = Z0 + lz;
       if (gx >= nx || gz >= nz) continue;
-      const size_t g = (size_t)gx * nz + gz;
+      const size_t g = (size_t)gx * nz + gz;   // unpadded (injection cells)
+      const size_t gp = (size_t)gx * ps + gz;  // padded
       float vx = sv[0][lx + 4][lz + 4], vz = sv[1][lx + 4][lz + 4];
       const float b = bb[k];
       if (gx >= 2 && gx < nx - 2 && gz >= 2 && gz < nz - 2) {
@@ -240,8 +243,8 @@ __global__ void __launch_bounds__(NT, 4) fused_step(const StepArgs a) {
       }
       if (p.n && gx >= p.x0 && gx < p.x0 + p.w && gz >= p.z0 && gz < p.z0 + p.h)
         inject(a, g, gx, gz, b, vx, vz);
-      a.out.vx[g] = vx;
-      a.out.vz[g] = vz;
+      a.out.vx[gp] = vx;
+      a.out.vz[gp] = vz;
     }
   }
 }
@@ -266,7 +269,7 @@ cudaError_t launch(const StepArgs &a, cudaStream_t s) {
 }
 
 cudaError_t zero(const SolverArgs &a, void *const second[5], cudaStream_t s) {
-  const size_t bytes = (size_t)a.nx * a.nz * sizeof(float);
+  const size_t bytes = (size_t)a.nx * a.pitch * sizeof(float);
   void *prim[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
   for (int f = 0; f < 5; ++f) {
     cudaError_t e = cudaMemsetAsync(prim[f], 0, bytes, s);
@@ -282,6 +285,7 @@ StepArgs base_step_args(const SolverArgs &a) {
   StepArgs s;
   s.nx = a.nx;
   s.nz = a.nz;
+  s.pitch = a.pitch;
   s.np = a.np;
   s.nt = a.nt;
   s.dt = (float)a.dt;

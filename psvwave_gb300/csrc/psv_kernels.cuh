@@ -25,9 +25,12 @@
 namespace psv {
 namespace kern {
 
+// Wave-field and medium arrays are stored with a row pitch (pitch >= nz,
+// a multiple of 4 points so rows start on 16-byte boundaries); snapshots,
+// kernels and injection cells use the reference's unpadded [nx][nz] index.
 template <typename T>
 struct Grid {
-  int nx, nz, np;
+  int nx, nz, np, pitch;
   T dt, dx, dz;
   T *vx, *vz, *txx, *tzz, *txz;
   const T *lm, *la, *mu, *b;
@@ -117,25 +120,26 @@ __global__ void __launch_bounds__(256) stress_step(Grid<T> g, StressExtras<T, AD
     }
   }
   if (ix >= g.nx || iz >= g.nz) return;
-  const int nz = g.nz;
-  const size_t i = (size_t)ix * nz + iz;
+  const int nz = g.nz, ps = g.pitch;
+  const size_t u = (size_t)ix * nz + iz;  // unpadded index
+  const size_t i = (size_t)ix * ps + iz;  // padded index
   T txx = g.txx[i], tzz = g.tzz[i], txz = g.txz[i];
   if (!ADJ && e.snap[0]) {
-    e.snap[0][i] = g.vx[i];
-    e.snap[1][i] = g.vz[i];
-    e.snap[2][i] = txx;
-    e.snap[3][i] = tzz;
-    e.snap[4][i] = txz;
+    e.snap[0][u] = g.vx[i];
+    e.snap[1][u] = g.vz[i];
+    e.snap[2][u] = txx;
+    e.snap[3][u] = tzz;
+    e.snap[4][u] = txz;
   }
   if (ADJ && e.asnap[0] && ix >= e.fx0 && ix < e.fx1 && iz >= e.fz0 && iz < e.fz1) {
-    Corr<T>::apply(e.sidt, g.lm[i], g.la[i], g.mu[i], e.asnap[0][i], e.asnap[1][i],
-                   e.asnap[2][i], e.asnap[3][i], e.asnap[4][i], g.vx[i], g.vz[i], txx, tzz,
-                   txz, e.krho + i, e.klam + i, e.kmu + i);
+    Corr<T>::apply(e.sidt, g.lm[i], g.la[i], g.mu[i], e.asnap[0][u], e.asnap[1][u],
+                   e.asnap[2][u], e.asnap[3][u], e.asnap[4][u], g.vx[i], g.vz[i], txx, tzz,
+                   txz, e.krho + u, e.klam + u, e.kmu + u);
   }
   if (ix < 2 || ix >= g.nx - 2 || iz < 2 || iz >= nz - 2) return;
   const T c1 = T(9.0 / 8.0), c2 = T(1.0 / 24.0);
   const T *vx = g.vx, *vz = g.vz;
-  const size_t xp1 = i + nz, xp2 = i + 2 * nz, xm1 = i - nz, xm2 = i - 2 * nz;
+  const size_t xp1 = i + ps, xp2 = i + 2 * ps, xm1 = i - ps, xm2 = i - 2 * ps;
   const size_t zp1 = i + 1, zp2 = i + 2, zm1 = i - 1, zm2 = i - 2;
   const T lm = g.lm[i], la = g.la[i], mu = g.mu[i];
   const T tp = taper_at(g, ix, iz);
@@ -192,18 +196,19 @@ __global__ void __launch_bounds__(256) velocity_step(Grid<T> g, InjArgs q) {
   const int iz = blockIdx.x * blockDim.x + threadIdx.x;
   const int ix = blockIdx.y * blockDim.y + threadIdx.y;
   if (ix >= g.nx || iz >= g.nz) return;
-  const int nz = g.nz;
+  const int nz = g.nz, ps = g.pitch;
   const bool interior = ix >= 2 && ix < g.nx - 2 && iz >= 2 && iz < nz - 2;
   const InjPlan &p = q.plan;
   const bool in_box = p.n && ix >= p.x0 && ix < p.x0 + p.w && iz >= p.z0 && iz < p.z0 + p.h;
   if (!interior && !in_box) return;
-  const size_t i = (size_t)ix * nz + iz;
+  const size_t u = (size_t)ix * nz + iz;  // unpadded index (injection cells)
+  const size_t i = (size_t)ix * ps + iz;  // padded index
   T vx = g.vx[i], vz = g.vz[i];
   const T b = g.b[i];
   if (interior) {
     const T c1 = T(9.0 / 8.0), c2 = T(1.0 / 24.0);
     const T *txx = g.txx, *tzz = g.tzz, *txz = g.txz;
-    const size_t xp1 = i + nz, xp2 = i + 2 * nz, xm1 = i - nz, xm2 = i - 2 * nz;
+    const size_t xp1 = i + ps, xp2 = i + 2 * ps, xm1 = i - ps, xm2 = i - 2 * ps;
     const size_t zp1 = i + 1, zp2 = i + 2, zm1 = i - 1, zm2 = i - 2;
     const T tp = taper_at(g, ix, iz);
     const T ax = (c1 * (txx[i] - txx[xm1]) + c2 * (txx[xm2] - txx[xp1])) / g.dx +
@@ -218,7 +223,7 @@ __global__ void __launch_bounds__(256) velocity_step(Grid<T> g, InjArgs q) {
       vz = tp * (vz - b * g.dt * az);
     }
   }
-  if (in_box) inject<T>(q, i, ix, iz, b, vx, vz);
+  if (in_box) inject<T>(q, u, ix, iz, b, vx, vz);
   g.vx[i] = vx;
   g.vz[i] = vz;
 }
@@ -245,16 +250,28 @@ __global__ void receiver_cumsum(int nr, int nt, int n_steps, double dt, double d
 // lm = vp^2 rho, la = lm - 2 mu, mu = vs^2 rho, b = 1 / rho, computed in FP64
 // (src/fdModel.cpp:1034-1051) and stored in T.
 template <typename T>
-__global__ void medium_kernel(int n, const double *vp, const double *vs, const double *rho,
-                              T *lm, T *la, T *mu, T *b) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double m = (vs[i] * vs[i]) * rho[i];
-  const double l = (vp[i] * vp[i]) * rho[i];
+__global__ void medium_kernel(int nx, int nz, int pitch, const double *vp, const double *vs,
+                              const double *rho, T *lm, T *la, T *mu, T *b) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nx * nz) return;
+  const int ix = u / nz, iz = u - ix * nz;
+  const size_t i = (size_t)ix * pitch + iz;
+  const double m = (vs[u] * vs[u]) * rho[u];
+  const double l = (vp[u] * vp[u]) * rho[u];
   mu[i] = (T)m;
   lm[i] = (T)l;
   la[i] = (T)(l - 2 * m);
-  b[i] = (T)(1.0 / rho[i]);
+  b[i] = (T)(1.0 / rho[u]);
+}
+
+// dst[ix][iz] (unpadded, FP64) = src[ix * pitch + iz].
+template <typename T>
+__global__ void unpad_kernel(int nx, int nz, int pitch, const T *src, double *dst) {
+  for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < (size_t)nx * nz;
+       u += (size_t)gridDim.x * blockDim.x) {
+    const size_t ix = u / nz, iz = u - ix * nz;
+    dst[u] = (double)src[ix * pitch + iz];
+  }
 }
 
 template <typename T>
@@ -280,6 +297,7 @@ kern::Grid<T> make_grid(const SolverArgs &a) {
   kern::Grid<T> g;
   g.nx = a.nx;
   g.nz = a.nz;
+  g.pitch = a.pitch;
   g.np = a.np;
   g.dt = (T)a.dt;
   g.dx = (T)a.dx;
@@ -299,7 +317,7 @@ kern::Grid<T> make_grid(const SolverArgs &a) {
 
 template <typename T>
 cudaError_t zero_fields(const SolverArgs &a, cudaStream_t s) {
-  const size_t bytes = (size_t)a.nx * a.nz * sizeof(T);
+  const size_t bytes = (size_t)a.nx * a.pitch * sizeof(T);
   void *f[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
   for (void *p : f) {
     cudaError_t e = cudaMemsetAsync(p, 0, bytes, s);
@@ -394,10 +412,20 @@ cudaError_t run_adjoint(const SolverArgs &a, const InjPlan &plan, int shot, cuda
 }
 
 template <typename T>
-cudaError_t run_medium(int n, const double *vp, const double *vs, const double *rho, void *lm,
-                       void *la, void *mu, void *b, cudaStream_t s) {
-  kern::medium_kernel<T><<<(n + 255) / 256, 256, 0, s>>>(n, vp, vs, rho, (T *)lm, (T *)la,
-                                                           (T *)mu, (T *)b);
+cudaError_t run_medium(int nx, int nz, int pitch, const double *vp, const double *vs,
+                       const double *rho, void *lm, void *la, void *mu, void *b, cudaStream_t s) {
+  const int n = nx * nz;
+  kern::medium_kernel<T><<<(n + 255) / 256, 256, 0, s>>>(nx, nz, pitch, vp, vs, rho, (T *)lm,
+                                                           (T *)la, (T *)mu, (T *)b);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t run_unpad(int nx, int nz, int pitch, const void *src, double *dst, cudaStream_t s) {
+  size_t blocks = ((size_t)nx * nz + 255) / 256;
+  if (blocks > 65535) blocks = 65535;
+  if (blocks == 0) return cudaSuccess;
+  kern::unpad_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(nx, nz, pitch, (const T *)src, dst);
   return cudaGetLastError();
 }
 
@@ -432,9 +460,14 @@ cudaError_t run_narrow(size_t n, const double *src, void *dst, cudaStream_t s) {
                                cudaStream_t s) {                                            \
     return run_adjoint<T>(a, plan, shot, s);                                                \
   }                                                                                         \
-  cudaError_t medium_##SUFFIX(int n, const double *vp, const double *vs, const double *rho, \
-                              void *lm, void *la, void *mu, void *b, cudaStream_t s) {      \
-    return run_medium<T>(n, vp, vs, rho, lm, la, mu, b, s);                                 \
+  cudaError_t medium_##SUFFIX(int nx, int nz, int pitch, const double *vp, const double *vs, \
+                              const double *rho, void *lm, void *la, void *mu, void *b,     \
+                              cudaStream_t s) {                                             \
+    return run_medium<T>(nx, nz, pitch, vp, vs, rho, lm, la, mu, b, s);                     \
+  }                                                                                         \
+  cudaError_t unpad_##SUFFIX(int nx, int nz, int pitch, const void *src, double *dst,       \
+                             cudaStream_t s) {                                              \
+    return run_unpad<T>(nx, nz, pitch, src, dst, s);                                        \
   }                                                                                         \
   cudaError_t widen_##SUFFIX(size_t n, const void *src, double *dst, cudaStream_t s) {     \
     return run_widen<T>(n, src, dst, s);                                                    \

@@ -88,6 +88,7 @@ Model::Model(const Config &cfg, int precision, int device)
   DeviceGuard guard(device_);
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   variant_ = prec_ == PSV_FP32 ? kFused : kTwoKernel;
+  pitch_ = (geo_.nz + 3) / 4 * 4;
   build_tables();
   allocate();
   build_tma_maps();
@@ -109,7 +110,7 @@ Model::Model(const Config &cfg, int precision, int device)
 
 Model::Model(const Model &o)
     : cfg_(o.cfg_), geo_(o.geo_), prec_(o.prec_), device_(o.device_), async_(o.async_),
-      misfit_(o.misfit_), variant_(o.variant_), cur_(o.cur_) {
+      misfit_(o.misfit_), pitch_(o.pitch_), variant_(o.variant_), cur_(o.cur_) {
   DeviceGuard guard(device_);
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   build_tables();
@@ -146,6 +147,7 @@ Model::Model(const Model &o)
 
 Model::~Model() {
   DeviceGuard guard(device_);
+  clear_graphs();
   if (stream_) {
     cudaStreamSynchronize(stream_);
     cudaStreamDestroy(stream_);
@@ -203,14 +205,14 @@ void Model::build_tables() {
 }
 
 void Model::allocate() {
-  const size_t g = grid_size(), e = elem(), d = data_size();
-  for (auto &f : fields_) f.allocate(g * e);
+  const size_t g = grid_size(), gp = padded_size(), e = elem(), d = data_size();
+  for (auto &f : fields_) f.allocate(gp * e);
   if (prec_ == PSV_FP32)
-    for (auto &f : fields2_) f.allocate(g * e);
-  lm_.allocate(g * e);
-  la_.allocate(g * e);
-  mu_.allocate(g * e);
-  b_.allocate(g * e);
+    for (auto &f : fields2_) f.allocate(gp * e);
+  lm_.allocate(gp * e);
+  la_.allocate(gp * e);
+  mu_.allocate(gp * e);
+  b_.allocate(gp * e);
   vp_.allocate(g * sizeof(double));
   vs_.allocate(g * sizeof(double));
   rho_.allocate(g * sizeof(double));
@@ -232,7 +234,7 @@ void Model::allocate() {
                           cudaMemcpyHostToDevice),
                "upload stf");
   std::vector<int> cells(cfg_.nr);
-  for (int r = 0; r < cfg_.nr; ++r) cells[r] = ix_rec_[r] * geo_.nz + iz_rec_[r];
+  for (int r = 0; r < cfg_.nr; ++r) cells[r] = ix_rec_[r] * pitch_ + iz_rec_[r];
   if (cfg_.nr)
     cuda_check(cudaMemcpy(rec_cell_.get(), cells.data(), cells.size() * sizeof(int),
                           cudaMemcpyHostToDevice),
@@ -330,14 +332,16 @@ void Model::build_plans() {
 
 void Model::build_tma_maps() {
   tma_ok_ = false;
-  if (prec_ != PSV_FP32 || !tma::supported(geo_.nx, geo_.nz)) return;
+  if (prec_ != PSV_FP32 || !tma::supported(geo_.nx, geo_.nz, pitch_)) return;
   const float *a[5], *b[5];
   for (int f = 0; f < 5; ++f) {
     a[f] = fields_[f].as<float>();
     b[f] = fields2_[f].as<float>();
   }
-  tma_ok_ = tma::make_maps(maps_[0], a, lm_.as<float>(), mu_.as<float>(), geo_.nx, geo_.nz) &&
-            tma::make_maps(maps_[1], b, lm_.as<float>(), mu_.as<float>(), geo_.nx, geo_.nz);
+  tma_ok_ = tma::make_maps(maps_[0], a, lm_.as<float>(), mu_.as<float>(), geo_.nx, geo_.nz,
+                           pitch_) &&
+            tma::make_maps(maps_[1], b, lm_.as<float>(), mu_.as<float>(), geo_.nx, geo_.nz,
+                           pitch_);
 }
 
 void Model::check_device_error() {
@@ -350,6 +354,47 @@ void Model::check_device_error() {
     cudaStreamSynchronize(stream());
     throw Error(PSV_ERR_CUDA, "a CTA timed out waiting for its TMA tile copies");
   }
+}
+
+void Model::clear_graphs() {
+  for (auto &kv : graphs_)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  graphs_.clear();
+}
+
+void Model::run_loop(int direction, int shot, bool store, int n_steps,
+                     const std::function<void()> &enqueue) {
+  if (!use_graphs_) {
+    enqueue();
+    return;
+  }
+  GraphEntry &g = graphs_[std::make_tuple(direction, shot, store ? 1 : 0, n_steps)];
+  if (g.exec) {
+    cuda_check(cudaGraphLaunch(g.exec, stream()), "cudaGraphLaunch");
+    cur_ = g.cur_after;
+    return;
+  }
+  if (g.uses++ == 0) {  // first run: eager (also sets per-device kernel attributes)
+    enqueue();
+    return;
+  }
+  cuda_check(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal),
+             "cudaStreamBeginCapture");
+  try {
+    enqueue();
+  } catch (...) {
+    cudaGraph_t broken = nullptr;
+    cudaStreamEndCapture(stream(), &broken);
+    if (broken) cudaGraphDestroy(broken);
+    throw;
+  }
+  cudaGraph_t graph = nullptr;
+  cuda_check(cudaStreamEndCapture(stream(), &graph), "cudaStreamEndCapture");
+  cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  cuda_check(e, "cudaGraphInstantiate");
+  g.cur_after = cur_;
+  cuda_check(cudaGraphLaunch(g.exec, stream()), "cudaGraphLaunch");
 }
 
 void Model::ensure_snapshots() {
@@ -389,6 +434,7 @@ SolverArgs Model::solver_args() {
   SolverArgs a;
   a.nx = geo_.nx;
   a.nz = geo_.nz;
+  a.pitch = pitch_;
   a.nt = cfg_.nt;
   a.np = cfg_.np_boundary;
   a.si = cfg_.snapshot_interval;
@@ -468,7 +514,7 @@ void Model::forward_simulate(int shot, bool store, bool verbose, bool output_wav
     cuda_check(e, "forward_simulate");
   };
   if (!output_wavefields) {
-    run(0, n_steps, true, true);
+    run_loop(0, shot, store, n_steps, [&] { run(0, n_steps, true, true); });
   } else {
     // Text dumps of vx, vz after every 10th step (src/fdModel.cpp:753-776).
     for (int it0 = 0; it0 < n_steps; it0 += 10) {
@@ -542,8 +588,7 @@ void Model::set_variant(int v) {
   if (prec_ == PSV_FP64 && v != kTwoKernel)
     throw Error(PSV_ERR_INVALID_ARGUMENT, "the fused variants are FP32 only");
   if (v == kFusedTma && !tma_ok_)
-    throw Error(PSV_ERR_INVALID_ARGUMENT,
-                "the TMA variant needs nz divisible by 4 (16-byte rows) and tensor-map support");
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "the TMA variant needs driver tensor-map support");
   DeviceGuard guard(device_);
   if ((v == kTwoKernel) != (variant_ == kTwoKernel) && cur_ == 1) {
     // Bring the current state back into the primary buffers.
@@ -554,6 +599,7 @@ void Model::set_variant(int v) {
     cur_ = 0;
   }
   variant_ = v;
+  clear_graphs();
   synchronize();
 }
 
@@ -571,19 +617,22 @@ void Model::adjoint_simulate(int shot, bool verbose) {
   auto t0 = std::chrono::steady_clock::now();
   void *second[5] = {fields2_[0].get(), fields2_[1].get(), fields2_[2].get(), fields2_[3].get(),
                      fields2_[4].get()};
-  cudaError_t e;
-  if (prec_ == PSV_FP64) {
-    e = adjoint_f64(a, plans_[cfg_.n_shots], shot, stream());
-  } else if (variant_ == kFusedTma) {
-    e = tma::adjoint(a, second, &cur_, maps_, err_flag_.as<int>(), plans_[cfg_.n_shots], shot,
-                     stream());
-  } else if (variant_ == kFused) {
-    e = fast::adjoint(a, second, &cur_, plans_[cfg_.n_shots], shot, stream());
-  } else {
-    e = adjoint_f32(a, plans_[cfg_.n_shots], shot, stream());
-    cur_ = 0;
-  }
-  cuda_check(e, "adjoint_simulate");
+  run_loop(1, shot, true, cfg_.nt, [&] {
+    cudaError_t e;
+    if (prec_ == PSV_FP64) {
+      e = adjoint_f64(a, plans_[cfg_.n_shots], shot, stream());
+      cur_ = 0;
+    } else if (variant_ == kFusedTma) {
+      e = tma::adjoint(a, second, &cur_, maps_, err_flag_.as<int>(), plans_[cfg_.n_shots], shot,
+                       stream());
+    } else if (variant_ == kFused) {
+      e = fast::adjoint(a, second, &cur_, plans_[cfg_.n_shots], shot, stream());
+    } else {
+      e = adjoint_f32(a, plans_[cfg_.n_shots], shot, stream());
+      cur_ = 0;
+    }
+    cuda_check(e, "adjoint_simulate");
+  });
   finish("adjoint_simulate");
   if (!async_ && variant_ == kFusedTma) check_device_error();
   if (verbose) {
@@ -658,13 +707,12 @@ void Model::run_model(bool verbose, bool simulate_adjoint) {
 
 void Model::update_from_velocity() {
   DeviceGuard guard(device_);
-  const int n = static_cast<int>(grid_size());
   cudaError_t e =
       prec_ == PSV_FP64
-          ? medium_f64(n, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(), lm_.get(),
-                       la_.get(), mu_.get(), b_.get(), stream())
-          : medium_f32(n, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(), lm_.get(),
-                       la_.get(), mu_.get(), b_.get(), stream());
+          ? medium_f64(geo_.nx, geo_.nz, pitch_, vp_.as<double>(), vs_.as<double>(),
+                       rho_.as<double>(), lm_.get(), la_.get(), mu_.get(), b_.get(), stream())
+          : medium_f32(geo_.nx, geo_.nz, pitch_, vp_.as<double>(), vs_.as<double>(),
+                       rho_.as<double>(), lm_.get(), la_.get(), mu_.get(), b_.get(), stream());
   cuda_check(e, "update_from_velocity");
   finish("update_from_velocity");
 }
@@ -822,19 +870,16 @@ void Model::get_wavefields(double *out[5]) {
   const size_t n = grid_size();
   DeviceBuffer *cur = (prec_ == PSV_FP32 && cur_ == 1) ? fields2_ : fields_;
   DeviceBuffer tmp;
-  if (prec_ != PSV_FP64) tmp.allocate(n * sizeof(double));
+  tmp.allocate(n * sizeof(double));
   for (int f = 0; f < 5; ++f) {
     if (!out[f]) continue;
-    if (prec_ == PSV_FP64) {
-      cuda_check(cudaMemcpyAsync(out[f], cur[f].get(), n * sizeof(double),
-                                 cudaMemcpyDeviceToHost, stream()),
-                 "get_wavefields");
-    } else {
-      widen(n, cur[f].get(), tmp.as<double>());
-      cuda_check(cudaMemcpyAsync(out[f], tmp.get(), n * sizeof(double), cudaMemcpyDeviceToHost,
-                                 stream()),
-                 "get_wavefields");
-    }
+    cudaError_t e = prec_ == PSV_FP64
+                        ? unpad_f64(geo_.nx, geo_.nz, pitch_, cur[f].get(), tmp.as<double>(), stream())
+                        : unpad_f32(geo_.nx, geo_.nz, pitch_, cur[f].get(), tmp.as<double>(), stream());
+    cuda_check(e, "get_wavefields");
+    cuda_check(cudaMemcpyAsync(out[f], tmp.get(), n * sizeof(double), cudaMemcpyDeviceToHost,
+                               stream()),
+               "get_wavefields");
     synchronize();
   }
 }

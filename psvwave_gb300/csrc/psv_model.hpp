@@ -5,7 +5,10 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
+#include <map>
 #include <memory>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -122,6 +125,10 @@ class Model {
   void set_stream(cudaStream_t s) { user_stream_ = s; }
   cudaStream_t stream() const { return user_stream_ ? user_stream_ : stream_; }
   void set_async(bool a) { async_ = a; }
+  void set_graphs(bool on) {
+    use_graphs_ = on;
+    if (!on) clear_graphs();
+  }
   void synchronize();
 
   enum DataKind { kSynthetic = 0, kObserved = 1, kAdjoint = 2 };
@@ -134,6 +141,9 @@ class Model {
   SolverArgs solver_args();
   void finish(const char *what);
   size_t grid_size() const { return static_cast<size_t>(geo_.nx) * geo_.nz; }
+  // Wave-field and medium arrays are stored with rows padded to pitch_ points
+  // (a multiple of 4, so every row starts on a 16-byte boundary).
+  size_t padded_size() const { return static_cast<size_t>(geo_.nx) * pitch_; }
   size_t data_size() const { return static_cast<size_t>(cfg_.n_shots) * cfg_.nr * cfg_.nt; }
   size_t elem() const { return prec_ == 1 ? sizeof(double) : sizeof(float); }
   void widen(size_t n, const void *src, double *dst_device);
@@ -154,12 +164,28 @@ class Model {
   std::vector<double> moment_;                          // [n_sources][2][2]
   std::vector<double> taper_tab_;                       // [np + 1]
 
+  int pitch_ = 0;
   int variant_ = kTwoKernel;
   int cur_ = 0;  // fused variants: 0 = fields_ hold the current state, 1 = fields2_
   bool tma_ok_ = false;   // TMA maps built for this model
   tma::Maps maps_[2];     // tensor maps of fields_ (0) and fields2_ (1) + medium
   void build_tma_maps();
   void check_device_error();
+
+  // Whole time loops captured as CUDA graphs, keyed by (direction, shot,
+  // store, steps). A loop runs eagerly the first time and is captured the
+  // second time, then replayed; the graph fixes every launch's arguments, so
+  // the cache is dropped whenever a kernel variant changes.
+  struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int uses = 0;
+    int cur_after = 0;
+  };
+  std::map<std::tuple<int, int, int, int>, GraphEntry> graphs_;
+  bool use_graphs_ = true;
+  void run_loop(int direction, int shot, bool store, int n_steps,
+                const std::function<void()> &enqueue);
+  void clear_graphs();
 
   // Device arrays.
   DeviceBuffer fields_[5];                    // vx vz txx tzz txz   (T)

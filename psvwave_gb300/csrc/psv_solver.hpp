@@ -42,16 +42,17 @@ struct InjPlan {
 // FP64 whatever T is.
 struct SolverArgs {
   int nx = 0, nz = 0, nt = 0, np = 0, si = 1, snapshots = 0, nr = 0;
+  int pitch = 0;  // row pitch of wave-field and medium arrays (>= nz, multiple of 4)
   double dt = 0, dx = 0, dz = 0;
-  // wave fields [nx][nz]
+  // wave fields [nx][pitch]
   void *vx = nullptr, *vz = nullptr, *txx = nullptr, *tzz = nullptr, *txz = nullptr;
-  // medium: lm = lambda + 2 mu, la = lambda, mu, b = 1 / rho  [nx][nz]
+  // medium: lm = lambda + 2 mu, la = lambda, mu, b = 1 / rho  [nx][pitch]
   const void *lm = nullptr, *la = nullptr, *mu = nullptr, *b = nullptr;
   // Cerjan taper by frame count, taper_tab[0..np] (src/fdModel.cpp:263-298)
   const void *taper_tab = nullptr;
   // stored forward snapshots, one array per field, [shots][snapshots][nx][nz]
   void *accu[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  // receivers: absolute cell, raw per-step velocities [2][nr][nt] (T)
+  // receivers: padded cell index ix * pitch + iz, raw per-step velocities [2][nr][nt] (T)
   const int *rec_cell = nullptr;
   void *rec_raw = nullptr;
   // seismograms, FP64 [shots][nr][nt]
@@ -81,8 +82,11 @@ enum Variant { kFused = 0, kTwoKernel = 1, kFusedTma = 2 };
                                bool finish, cudaStream_t s);                              \
   cudaError_t adjoint_##SUFFIX(const SolverArgs &a, const InjPlan &plan, int shot,       \
                                cudaStream_t s);                                           \
-  cudaError_t medium_##SUFFIX(int n, const double *vp, const double *vs, const double *rho, \
-                              void *lm, void *la, void *mu, void *b, cudaStream_t s);     \
+  cudaError_t medium_##SUFFIX(int nx, int nz, int pitch, const double *vp, const double *vs, \
+                              const double *rho, void *lm, void *la, void *mu, void *b,   \
+                              cudaStream_t s);                                            \
+  cudaError_t unpad_##SUFFIX(int nx, int nz, int pitch, const void *src, double *dst,     \
+                             cudaStream_t s);                                             \
   cudaError_t widen_##SUFFIX(size_t n, const void *src, double *dst, cudaStream_t s);    \
   cudaError_t narrow_##SUFFIX(size_t n, const double *src, void *dst, cudaStream_t s);
 PSV_SOLVER_DECLS(f32)

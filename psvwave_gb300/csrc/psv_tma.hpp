@@ -14,13 +14,14 @@ struct Maps {
   CUtensorMap vx, vz, txx, tzz, txz, lm, mu;
 };
 
-// True when the grid can use the TMA kernel (rows of a multiple of 16 bytes)
-// and the driver exposes tensor-map encoding.
-bool supported(int nx, int nz);
+// True when the arrays can use the TMA kernel (row pitch a multiple of 4
+// points, i.e. rows on 16-byte boundaries) and the driver exposes
+// tensor-map encoding.
+bool supported(int nx, int nz, int pitch);
 
 // Encodes the maps of one buffer set; false on failure.
 bool make_maps(Maps &m, const float *const fields[5], const float *lm, const float *mu, int nx,
-               int nz);
+               int nz, int pitch);
 
 // Time loops as fast::forward / fast::adjoint; maps[0] covers the primary
 // buffer set, maps[1] the second. *err (device int) is raised when a CTA's

@@ -1,4 +1,4 @@
-// FP32 fused time step with TMA tile loads (grids with nz % 4 == 0).
+// FP32 fused time step with TMA tile loads (rows padded to a multiple of 4 points).
 //
 // Same step as psv_fast_f32.cu -- new stresses over the tile plus a 2-point
 // halo, then new velocities of the tile's own points, over ping-pong buffers
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(NT, 3)
   float(*const smu)[W] = stile(4);
   uint64_t *bar = reinterpret_cast<uint64_t *>(base + kTileBytes);
 
-  const int nx = a.nx, nz = a.nz;
+  const int nx = a.nx, nz = a.nz, ps = a.pitch;
   const int X0 = blockIdx.y * TX, Z0 = blockIdx.x * TZ;
   const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
 
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(NT, 3)
 #pragma unroll
   for (int k = 0; k < KC; ++k) {
     const int gx = X0 + q + 4 * k;
-    bb[k] = (col_ok && gx < nx) ? __ldg(a.b + gx * nz + gzc) : 0.f;
+    bb[k] = (col_ok && gx < nx) ? __ldg(a.b + gx * ps + gzc) : 0.f;
   }
 
   // Bounded wait (about a second at most); the CTA agrees on the outcome so
@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(NT, 3)
       const int r = q + 4 * k;  // box row
       const int gx = X0 - 2 + r;
       if (!z_in || gx < 0 || gx >= nx) continue;
-      const int g = gx * nz + gz;
+      const int g = gx * nz + gz;   // unpadded (snapshots, kernels)
+      const int gp = gx * ps + gz;  // padded (wave fields)
       const int vr = r + 2;  // same point in the velocity box
       float sxx = sxx_[r][c], szz = szz_[r][c], sxz = sxz_[r][c];
       const bool own = z_own && r >= 2 && r < TX + 2;
@@ -227,8 +228,9 @@ __global__ void __launch_bounds__(NT, 3)
                           (c1 * (VZ[vr][c] - VZ[vr - 1][c]) +
                            c2 * (VZ[vr - 2][c] - VZ[vr + 1][c])) * a.idx;
         const float ex = dvx * a.idx, ez = dvz * a.idz;
-        const int cnt = min(min(tz, min(gx + 1, nx - gx)), a.np);
-        const float tp = a.taper_tab[cnt];
+        // Points at least np frames deep have taper exp(0) = 1 exactly.
+        const int cnt = min(tz, min(gx + 1, nx - gx));
+        const float tp = cnt < a.np ? __ldg(a.taper_tab + cnt) : 1.0f;
         sxx = tp * (sxx + dtv * (lm * ex + la * ez));
         szz = tp * (szz + dtv * (la * ex + lm * ez));
         sxz = tp * (sxz + dtv * mu * gxz);
@@ -237,9 +239,9 @@ __global__ void __launch_bounds__(NT, 3)
         sxz_[r][c] = sxz;
       }
       if (own) {
-        a.out.txx[g] = sxx;
-        a.out.tzz[g] = szz;
-        a.out.txz[g] = sxz;
+        a.out.txx[gp] = sxx;
+        a.out.tzz[gp] = szz;
+        a.out.txz[gp] = sxz;
       }
     }
   }
@@ -260,7 +262,8 @@ __global__ void __launch_bounds__(NT, 3)
       const int lx = q + 4 * k;
       const int gx = X0 + lx;
       if (gx >= nx) continue;
-      const int g = gx * nz + gzc;
+      const int g = gx * nz + gzc;   // unpadded (injection cells)
+      const int gp = gx * ps + gzc;  // padded
       const int r = lx + 2;  // stress box row
       float vx = sv[0][lx + 4][c], vz = sv[1][lx + 4][c];
       const float b = bb[k];
@@ -269,15 +272,15 @@ __global__ void __launch_bounds__(NT, 3)
                          (c1 * (TXZ[r][c] - TXZ[r][c - 1]) + c2 * (TXZ[r][c - 2] - TXZ[r][c + 1])) * a.idz;
         const float az = (c1 * (TXZ[r + 1][c] - TXZ[r][c]) + c2 * (TXZ[r - 1][c] - TXZ[r + 2][c])) * a.idx +
                          (c1 * (TZZ[r][c + 1] - TZZ[r][c]) + c2 * (TZZ[r][c - 1] - TZZ[r][c + 2])) * a.idz;
-        const int cnt = min(min(tz, min(gx + 1, nx - gx)), a.np);
-        const float tp = a.taper_tab[cnt];
+        const int cnt = min(tz, min(gx + 1, nx - gx));
+        const float tp = cnt < a.np ? __ldg(a.taper_tab + cnt) : 1.0f;
         const float bdt = b * dtv;
         vx = tp * (vx + bdt * ax);
         vz = tp * (vz + bdt * az);
       }
       if (z_box && gx >= p.x0 && gx < p.x0 + p.w) inject(a, g, gx, gzc, b, vx, vz);
-      a.out.vx[g] = vx;
-      a.out.vz[g] = vz;
+      a.out.vx[gp] = vx;
+      a.out.vz[gp] = vz;
     }
   }
 }
@@ -318,11 +321,11 @@ EncodeTiled encoder() {
   return fn;
 }
 
-bool encode(CUtensorMap *m, const float *ptr, int nx, int nz, int rows) {
+bool encode(CUtensorMap *m, const float *ptr, int nx, int nz, int pitch, int rows) {
   EncodeTiled fn = encoder();
   if (!fn) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)nz, (cuuint64_t)nx};
-  const cuuint64_t strides[1] = {(cuuint64_t)nz * sizeof(float)};
+  const cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
   const cuuint32_t box[2] = {(cuuint32_t)W, (cuuint32_t)rows};
   const cuuint32_t elem[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(ptr), dims, strides, box,
@@ -333,21 +336,25 @@ bool encode(CUtensorMap *m, const float *ptr, int nx, int nz, int rows) {
 
 }  // namespace
 
-bool supported(int nx, int nz) { return nz % 4 == 0 && nx > 0 && nz > 0 && encoder() != nullptr; }
+bool supported(int nx, int nz, int pitch) {
+  return pitch % 4 == 0 && pitch >= nz && nx > 0 && nz > 0 && encoder() != nullptr;
+}
 
 bool make_maps(Maps &m, const float *const fields[5], const float *lm, const float *mu, int nx,
-               int nz) {
-  return encode(&m.vx, fields[0], nx, nz, VR) && encode(&m.vz, fields[1], nx, nz, VR) &&
-         encode(&m.txx, fields[2], nx, nz, SR) && encode(&m.tzz, fields[3], nx, nz, SR) &&
-         encode(&m.txz, fields[4], nx, nz, SR) && encode(&m.lm, lm, nx, nz, SR) &&
-         encode(&m.mu, mu, nx, nz, SR);
+               int nz, int pitch) {
+  return encode(&m.vx, fields[0], nx, nz, pitch, VR) &&
+         encode(&m.vz, fields[1], nx, nz, pitch, VR) &&
+         encode(&m.txx, fields[2], nx, nz, pitch, SR) &&
+         encode(&m.tzz, fields[3], nx, nz, pitch, SR) &&
+         encode(&m.txz, fields[4], nx, nz, pitch, SR) && encode(&m.lm, lm, nx, nz, pitch, SR) &&
+         encode(&m.mu, mu, nx, nz, pitch, SR);
 }
 
 cudaError_t forward(const SolverArgs &a, void *const second[5], int *cur, const Maps maps[2],
                     int *err, const InjPlan &plan, int shot, bool store, int it0, int it1,
                     bool zero_first, bool finish, cudaStream_t s) {
   if (zero_first) {
-    const size_t bytes = (size_t)a.nx * a.nz * sizeof(float);
+    const size_t bytes = (size_t)a.nx * a.pitch * sizeof(float);
     void *prim[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
     for (int f = 0; f < 5; ++f) {
       cudaError_t e = cudaMemsetAsync(prim[f], 0, bytes, s);
@@ -389,7 +396,7 @@ cudaError_t forward(const SolverArgs &a, void *const second[5], int *cur, const 
 
 cudaError_t adjoint(const SolverArgs &a, void *const second[5], int *cur, const Maps maps[2],
                     int *err, const InjPlan &plan, int shot, cudaStream_t s) {
-  const size_t bytes = (size_t)a.nx * a.nz * sizeof(float);
+  const size_t bytes = (size_t)a.nx * a.pitch * sizeof(float);
   void *prim[5] = {a.vx, a.vz, a.txx, a.tzz, a.txz};
   for (int f = 0; f < 5; ++f) {
     cudaError_t e = cudaMemsetAsync(prim[f], 0, bytes, s);

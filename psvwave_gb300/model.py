@@ -391,6 +391,10 @@ class fdModel:
     def set_async(self, async_calls=True):
         _capi.check(self._lib.psv_set_async(self._h, int(bool(async_calls))))
 
+    def set_graph_capture(self, enable=True):
+        """Replay repeated time loops as CUDA graphs (default on)."""
+        _capi.check(self._lib.psv_set_graph_capture(self._h, int(bool(enable))))
+
     def synchronize(self):
         _capi.check(self._lib.psv_synchronize(self._h))
 
@@ -414,8 +418,8 @@ class fdModel:
 
     @property
     def kernel_variant(self):
-        """'fused_tma' (one launch per step with TMA tile loads; FP32 grids
-        with nz % 4 == 0), 'fused' (one launch per step, FP32) or
+        """'fused_tma' (one launch per step with TMA tile loads; the FP32
+        default), 'fused' (one launch per step, FP32) or
         'two_kernel' (stress and velocity launches; the FP64 variant)."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_get_kernel_variant(self._h, ctypes.byref(v)))

@@ -205,3 +205,30 @@ def test_descent_decreases_misfit():
         m.run_model(False, True)
         misfits.append(m.misfit)
     assert misfits[0] > misfits[-1]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_graph_replay_matches_eager(golden, precision):
+    """Repeated forward/adjoint loops replayed as CUDA graphs give the same
+    bits as kernel-by-kernel launches."""
+    res = []
+    for graphs in (False, True):
+        m = psv.fdModel(SMALL_INI, precision=precision)
+        m.set_graph_capture(graphs)
+        m.set_parameter_fields(*golden["target"])
+        for _ in range(3):  # eager, capture, replay
+            for s in range(m.n_shots):
+                m.forward_simulate(s, True)
+        m.set_observed_data(*m.get_synthetic_data())
+        m.set_parameter_fields(*golden["start"])
+        for _ in range(3):
+            for s in range(m.n_shots):
+                m.forward_simulate(s, True)
+            m.calculate_l2_adjoint_sources()
+            m.reset_kernels()
+            for s in range(m.n_shots):
+                m.adjoint_simulate(s)
+        m.map_kernels_to_velocity()
+        res.append((m.get_synthetic_data()[0], m.get_kernels()[1], m.get_wavefields()[0]))
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a, b)

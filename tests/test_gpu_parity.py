@@ -155,12 +155,14 @@ def test_fp32_vs_fp64_gpu_nb2_full_outputs():
         assert e <= FP32_TOL, (k, e)
 
 
-def test_default_fp32_variant_depends_on_row_alignment():
+def test_default_variants():
+    """FP32 models use the TMA step whatever nz is (rows are padded to 16
+    bytes: nz = 56 and nz = 150 alike); FP64 models the two-kernel step."""
     assert psv.fdModel(SMALL_INI).kernel_variant == "fused_tma"   # nz = 56
-    assert psv.fdModel(NB2_INI).kernel_variant == "fused"         # nz = 150
+    assert psv.fdModel(NB2_INI).kernel_variant == "fused_tma"     # nz = 150, padded to 152
     assert psv.fdModel(SMALL_INI, precision="fp64").kernel_variant == "two_kernel"
     with pytest.raises(ValueError):
-        psv.fdModel(NB2_INI).kernel_variant = "fused_tma"
+        psv.fdModel(SMALL_INI, precision="fp64").kernel_variant = "fused_tma"
 
 
 @pytest.mark.parametrize("variant", ["fused_tma", "fused", "two_kernel"])
