@@ -40,12 +40,27 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="skip the FWI-gradient and batching measurements")
+    p.add_argument("--ncu-case", type=int, default=0, metavar="NT",
+                   help="run one NT-step forward of the c1 workload and exit (for ncu captures)")
     return p.parse_args()
 
 
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
             int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def measured_traffic(kernel):
+    """DRAM bytes (read + write) per launch of `kernel` from the warm-cache
+    ncu capture summarised in profiles/<kernel>_c1.json, or None."""
+    path = os.path.join(ROOT, "profiles", "%s_c1.json" % kernel)
+    try:
+        with open(path) as f:
+            return float(json.load(f)["dram_bytes_per_launch"])
+    except Exception:
+        return None
 
 
 def measured_peaks():
@@ -134,6 +149,98 @@ def cpu_baseline(params_fn, media, seconds=12.0):
                       "%d of 5000 time steps, %.1f s" % (nx, nz, n, dt)}
 
 
+def fwi_gradients(steps, warmup, with_cpu):
+    """FWI gradients/s on the c0 workload: observed data from the target
+    medium, then each step is one full gradient at the start medium
+    (run_model: forward with snapshots, misfit, adjoint sources, kernel
+    reset, adjoint with kernel correlation, velocity mapping; FP32 wave fields,
+    FP64 misfit and kernels), timed end to end with the model's stream
+    synchronised, plus the gradient vector read back to the host."""
+    import psvwave_gb300 as psv
+    from psvwave_gb300 import workloads
+
+    p = workloads.c0_params()
+    target, start = workloads.c0_media()
+    m = psv.fdModel.from_parameters(p)
+    m.set_parameter_fields(*target)
+    for s_ in range(m.n_shots):
+        m.forward_simulate(s_, False)
+    m.set_observed_data(*m.get_synthetic_data())
+    m.set_parameter_fields(*start)
+    for _ in range(warmup):
+        m.run_model(False, True)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        m.run_model(False, True)
+        g = m.get_gradient_vector()
+    dt = time.perf_counter() - t0
+    out = {"value": steps / dt, "unit": "FWI gradients/s",
+           "workload": "c0: 250x150 grid, nt=4000, 2 sources in 1 shot, 19 receivers, "
+                       "snapshot interval 10; forward + misfit + adjoint + kernels per gradient",
+           "ms_per_gradient": 1e3 * dt / steps, "misfit": m.misfit,
+           "tile_shape": m.tile_shape}
+    if with_cpu:
+        from oracle import portbind
+        o = portbind.OracleModel(params=p)
+        o.set_parameter_fields(*target)
+        o.forward_simulate(0, False)
+        o.set_observed_data(*o.get_synthetic_data())
+        o.set_parameter_fields(*start)
+        t0 = time.perf_counter()
+        o.run_model(True)
+        cdt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / cdt, "unit": "FWI gradients/s",
+                               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                               "kind": "port", "sample": "one full c0 gradient, %.2f s" % cdt}
+        out["cpu_misfit"] = o.misfit
+    return out
+
+
+def batched(steps, warmup):
+    """Aggregate Gcell-updates/s of the batching workload (256 models of
+    uneven sizes, 1-4 shots each, nt = 1000): all shots of all models in one
+    launch per time step (one CUDA graph), versus the same models run one
+    after another, each shot its own forward_simulate."""
+    import psvwave_gb300 as psv
+    from psvwave_gb300 import workloads
+
+    models = []
+    for p, media in workloads.c2_models():
+        m = psv.fdModel.from_parameters(p)
+        m.set_parameter_fields(*media)
+        models.append(m)
+    b = psv.Batch()
+    for m in models:
+        b.add_all_shots(m)
+    shape = b.autotune(50)
+    info = b.info()  # after the build, so the tile count is known
+    nt = models[0].nt
+    for _ in range(max(2, warmup)):
+        b.forward()
+    b_times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        b.forward()
+        b_times.append(time.perf_counter() - t0)
+    batched_rate = info["cells"] * nt / (sum(b_times) / len(b_times)) / 1e9
+    for m in models:  # warm the per-model graphs
+        for _ in range(2):
+            for s_ in range(m.n_shots):
+                m.forward_simulate(s_, False)
+    t0 = time.perf_counter()
+    for m in models:
+        for s_ in range(m.n_shots):
+            m.forward_simulate(s_, False)
+    seq = time.perf_counter() - t0
+    seq_rate = info["cells"] * nt / seq / 1e9
+    return {"value": batched_rate, "unit": "Gcell-updates/s",
+            "workload": "c2: 256 seeded models, nx_inner U[200,800], nz_inner U[100,400], "
+                        "25-cell boundary, 1-4 shots, Ricker 20-50 Hz, nt=1000, forward only",
+            "members": info["members"], "cells_per_step": info["cells"], "tiles": info["tiles"],
+            "tile_shape": shape, "one_launch_per_model": seq_rate,
+            "speedup_vs_one_launch_per_model": batched_rate / seq_rate}
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -162,8 +269,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def ncu_case(nt):
+    """A short forward run of the c1 workload, for ncu captures."""
+    import psvwave_gb300 as psv
+    from psvwave_gb300 import workloads
+
+    m = psv.fdModel.from_parameters(workloads.c1_params(nt=nt))
+    m.set_parameter_fields(*workloads.c1_media())
+    m.forward_simulate(0, False)
+    print("ncu case: %s, %s tiles, seismogram sum %.6e" % (
+        m.kernel_variant, m.tile_shape, m.get_synthetic_data()[0].sum()))
+
+
 def main():
     args = parse()
+    if args.ncu_case:
+        ncu_case(args.ncu_case)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
@@ -257,12 +379,18 @@ def main():
     peak, peak_kind = measured_peaks()
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": None, "bytes_per_launch": bpc * cells,
-                "kernel_ms": kernel_ms, "step_ms": per_step_ms}
+                "traffic": measured_traffic(dominant), "bytes_per_launch": bpc * cells,
+                "kernel_ms": kernel_ms, "step_ms": per_step_ms,
+                "achieved_gcells_per_kernel": cells / (kernel_ms[dominant] / 1e3) / 1e9}
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(workloads.c1_params, media)
+    secondary = None
+    if rank == 0 and not args.no_secondary:
+        secondary = {"fwi_gradients": fwi_gradients(args.steps, args.warmup,
+                                                    world == 1 and not args.no_cpu_baseline),
+                     "batched": batched(args.steps, args.warmup)}
 
     if rank == 0:
         line = {
@@ -277,10 +405,11 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": (2 * nt + 1) * args.steps,
+            "gpu_launches": (len(kernel_ms) * nt + 1) * args.steps,
             "roofline": roofline,
             "cpu_baseline": base,
             "clocks": clocks,
+            "secondary": secondary,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

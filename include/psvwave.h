@@ -245,6 +245,51 @@ enum psv_variant { PSV_VARIANT_FUSED = 0, PSV_VARIANT_TWO_KERNEL = 1, PSV_VARIAN
 int psv_set_kernel_variant(psv_model *m, int variant);
 int psv_get_kernel_variant(const psv_model *m, int *variant);
 
+/* Tile shape of the FP32 TMA step: PSV_TILE_32X60 (x rows by z columns;
+ * large grids) or PSV_TILE_16X28 (small grids; chosen by default below
+ * 400,000 grid points). psv_autotune times every shape on n_steps forward
+ * steps of shot 0 and keeps the fastest in *chosen. No counterpart in the
+ * reference. */
+enum psv_tile_shape { PSV_TILE_32X60 = 0, PSV_TILE_16X28 = 1 };
+int psv_set_tile_shape(psv_model *m, int shape);
+int psv_get_tile_shape(const psv_model *m, int *shape);
+int psv_autotune(psv_model *m, int n_steps, int *chosen);
+
+/* ---- exact discrete adjoint --------------------------------------------- */
+/* Gradient of the L2 misfit (src/fdModel.cpp:1128-1145) over all shots with
+ * respect to vp, vs and rho by the exact discrete adjoint: the transpose of
+ * the time-stepping operator, run backwards. Unlike the reference's adjoint
+ * (src/fdModel.cpp:789-969, a reverse-time re-run of the forward scheme),
+ * it agrees with finite differences of the discrete misfit. Forward states
+ * are rebuilt from checkpoints taken every `checkpoint_every` steps
+ * (checkpoint_every >= nt keeps every state of the run). *misfit receives the
+ * misfit; the gradient ([nx][nz] each) is read with psv_get_exact_gradient
+ * (host) or psv_get_exact_gradient_device. psv_exact_bytes estimates the
+ * device memory of a given checkpoint interval. */
+int psv_exact_gradient(psv_model *m, int checkpoint_every, double *misfit);
+int psv_get_exact_gradient(psv_model *m, double *g_vp, double *g_vs, double *g_rho);
+int psv_get_exact_gradient_device(psv_model *m, double *g_vp, double *g_vs, double *g_rho);
+int psv_exact_bytes(const psv_model *m, int checkpoint_every, size_t *bytes);
+
+/* ---- batched simulation --------------------------------------------------- */
+/* A batch advances shots of many FP32 models -- of uneven grid sizes -- in
+ * one TMA-step launch per time step, the whole time loop replayed as one CUDA
+ * graph. Members must share nt and live on the batch's device; models must
+ * outlive the batch. Seismograms (and, with store_fields, snapshots) land in
+ * each member model's own arrays for that shot, as forward_simulate would
+ * leave them. No counterpart in the reference, which runs one shot of one
+ * model at a time (src/fdModel.cpp:1293-1296). */
+typedef struct psv_batch psv_batch;
+int psv_batch_create(int device, psv_batch **out);
+int psv_batch_destroy(psv_batch *b);
+int psv_batch_add(psv_batch *b, psv_model *m, int i_shot);
+/* Forward simulation of every member over its first n_steps steps (all if
+ * n_steps <= 0). */
+int psv_batch_forward(psv_batch *b, int store_fields, int n_steps);
+int psv_batch_set_tile_shape(psv_batch *b, int shape);
+int psv_batch_autotune(psv_batch *b, int n_steps, int *chosen);
+int psv_batch_info(const psv_batch *b, int *members, int *tiles, double *cells);
+
 /* ---- no-allocation entry point ------------------------------------------ */
 /* L2 misfit 0.5 dt sum((obs - syn)^2) over both components, written to the
  * device double *misfit, from caller-owned device arrays of n samples each

@@ -7,7 +7,8 @@ finite-difference solver, behind the reference's `fdModel` API.
     ux, uz = model.get_synthetic_data()
 """
 from .config import from_dictionary, get_dictionary, to_parameters, write_dictionary
+from .batch import Batch
 from .model import fdModel
 
-__all__ = ["fdModel", "get_dictionary", "write_dictionary", "from_dictionary", "to_parameters"]
+__all__ = ["fdModel", "Batch", "get_dictionary", "write_dictionary", "from_dictionary", "to_parameters"]
 __version__ = "0.1.0"

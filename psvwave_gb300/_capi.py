@@ -113,6 +113,20 @@ _SIGNATURES = {
     "psv_step_kernel_name": [_vp, _c_int],
     "psv_set_kernel_variant": [_vp, _c_int],
     "psv_get_kernel_variant": [_vp, _ip],
+    "psv_set_tile_shape": [_vp, _c_int],
+    "psv_get_tile_shape": [_vp, _ip],
+    "psv_autotune": [_vp, _c_int, _ip],
+    "psv_exact_gradient": [_vp, _c_int, _dp],
+    "psv_get_exact_gradient": [_vp, _dp, _dp, _dp],
+    "psv_get_exact_gradient_device": [_vp, _vp, _vp, _vp],
+    "psv_exact_bytes": [_vp, _c_int, ctypes.POINTER(ctypes.c_size_t)],
+    "psv_batch_create": [_c_int, ctypes.POINTER(_vp)],
+    "psv_batch_destroy": [_vp],
+    "psv_batch_add": [_vp, _vp, _c_int],
+    "psv_batch_forward": [_vp, _c_int, _c_int],
+    "psv_batch_set_tile_shape": [_vp, _c_int],
+    "psv_batch_autotune": [_vp, _c_int, _ip],
+    "psv_batch_info": [_vp, _ip, _ip, _dp],
     "psv_l2_misfit_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_size_t, _c_double, _vp, _vp],
 }
 _RESTYPES = {"psv_last_error": ctypes.c_char_p, "psv_step_kernel_name": ctypes.c_char_p}

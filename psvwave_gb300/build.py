@@ -35,6 +35,7 @@ UNITS = [
     ("psv_noalloc.cu", []),
     ("psv_config.cpp", []),
     ("psv_model.cpp", []),
+    ("psv_batch.cpp", []),
     ("psv_capi.cpp", []),
 ]
 

@@ -66,6 +66,30 @@ __global__ void lame_to_velocity(size_t n, const double *vp, const double *vs,
   }
 }
 
+__global__ void reverse_residual_sum(int rows, int nt, double dt, double dxdz, const double *syn,
+                                     const double *obs, double *adj) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  const size_t off = (size_t)r * nt;
+  double acc = 0;
+  for (int n = nt - 1; n >= 0; --n) {
+    acc += dt * (syn[off + n] - obs[off + n]);
+    adj[off + n] = dt / dxdz * acc;
+  }
+}
+
+__global__ void chain_to_velocity(size_t n, const double *vp, const double *vs, const double *rho,
+                                  const double *glm, const double *gla, const double *gmu,
+                                  const double *gb, double *gvp, double *gvs, double *grho) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double p = vp[i], s = vs[i], r = rho[i];
+    gvp[i] = 2.0 * r * p * (glm[i] + gla[i]);
+    gvs[i] = 2.0 * r * s * gmu[i] - 4.0 * r * s * gla[i];
+    grho[i] = p * p * glm[i] + (p * p - 2.0 * s * s) * gla[i] + s * s * gmu[i] - gb[i] / (r * r);
+  }
+}
+
 unsigned blocks_for(size_t n) {
   size_t b = (n + 255) / 256;
   if (b > 4096) b = 4096;
@@ -74,6 +98,22 @@ unsigned blocks_for(size_t n) {
 }
 
 }  // namespace
+
+cudaError_t exact_receiver_terms(int rows, int nt, double dt, double dxdz, const double *syn,
+                                 const double *obs, double *adj, cudaStream_t s) {
+  if (rows <= 0) return cudaSuccess;
+  reverse_residual_sum<<<(rows + 127) / 128, 128, 0, s>>>(rows, nt, dt, dxdz, syn, obs, adj);
+  return cudaGetLastError();
+}
+
+cudaError_t exact_chain(size_t n, const double *vp, const double *vs, const double *rho,
+                        const double *g_lm, const double *g_la, const double *g_mu,
+                        const double *g_b, double *g_vp, double *g_vs, double *g_rho,
+                        cudaStream_t s) {
+  chain_to_velocity<<<blocks_for(n), 256, 0, s>>>(n, vp, vs, rho, g_lm, g_la, g_mu, g_b, g_vp,
+                                                  g_vs, g_rho);
+  return cudaGetLastError();
+}
 
 cudaError_t misfit_l2(size_t n, double dt, const double *obs_ux, const double *syn_ux,
                       const double *obs_uz, const double *syn_uz, double *partials,

@@ -1,0 +1,253 @@
+// Batched forward simulation of many (model, shot) members; see psv_batch.hpp.
+#include "psv_batch.hpp"
+
+#include <algorithm>
+
+#include "../../include/psvwave.h"
+
+namespace psv {
+
+Batch::Batch(int device) : device_(device) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    throw Error(PSV_ERR_CUDA, "no CUDA device is available");
+  }
+  if (device < 0 || device >= count) throw Error(PSV_ERR_INVALID_ARGUMENT, "CUDA device index out of range");
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  err_flag_.allocate(sizeof(int));
+  cudaSetDevice(prev);
+}
+
+Batch::~Batch() {
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(device_);
+  clear_graphs();
+  if (stream_) {
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+  }
+  cudaSetDevice(prev);
+}
+
+void Batch::clear_graphs() {
+  if (graph_.exec) cudaGraphExecDestroy(graph_.exec);
+  graph_ = Graph();
+}
+
+void Batch::add(Model *m, int shot) {
+  if (!m) throw Error(PSV_ERR_INVALID_ARGUMENT, "model must not be NULL");
+  if (m->precision() != PSV_FP32 || !m->tma_ok_)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "batched simulation needs FP32 models with the TMA step");
+  if (m->device() != device_) throw Error(PSV_ERR_INVALID_ARGUMENT, "model lives on another device");
+  if (shot < 0 || shot >= m->config().n_shots)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "i_shot out of range");
+  if (!members_.empty() && m->config().nt != nt_)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "all members of a batch must share nt");
+  nt_ = m->config().nt;
+  members_.emplace_back(m, shot);
+  built_ = false;
+  clear_graphs();
+}
+
+double Batch::cells() const {
+  double c = 0;
+  for (const auto &mb : members_)
+    c += static_cast<double>(mb.first->geometry().nx) * mb.first->geometry().nz;
+  return c;
+}
+
+void Batch::build() {
+  size_t arena = 0, raw = 0;
+  raw_off_.clear();
+  for (const auto &mb : members_) {
+    arena += 10 * mb.first->padded_size();
+    raw_off_.push_back(raw);
+    raw += 2 * static_cast<size_t>(mb.first->config().nr) * nt_;
+  }
+  arena_.allocate(arena * sizeof(float));
+  raw_.allocate(std::max<size_t>(raw, 1) * sizeof(float));
+  std::vector<tma::SimDesc> descs(members_.size());
+  std::vector<int4> tiles[tma::kNumTileCfgs];
+  float *next = arena_.as<float>();
+  for (size_t k = 0; k < members_.size(); ++k) {
+    Model &m = *members_[k].first;
+    const int shot = members_[k].second;
+    const Config &c = m.config();
+    const Geometry &g = m.geometry();
+    const size_t gp = m.padded_size();
+    tma::SimDesc &d = descs[k];
+    for (int s = 0; s < 2; ++s) {
+      float *f[5];
+      for (int i = 0; i < 5; ++i, next += gp) f[i] = next;
+      d.set[s] = fast::Fields{f[0], f[1], f[2], f[3], f[4]};
+    }
+    d.nx = g.nx;
+    d.nz = g.nz;
+    d.pitch = m.pitch_;
+    d.np = c.np_boundary;
+    d.nt = c.nt;
+    d.nr = c.nr;
+    d.si = c.snapshot_interval;
+    d.dt = static_cast<float>(c.dt);
+    d.idx = static_cast<float>(1.0 / c.dx);
+    d.idz = static_cast<float>(1.0 / c.dz);
+    d.dt_d = c.dt;
+    d.lm = m.lm_.as<float>();
+    d.b = m.b_.as<float>();
+    d.taper_tab = m.taper_tab_d_.as<float>();
+    for (int f = 0; f < 5; ++f)
+      d.accu[f] = m.accu_[f].get() ? m.accu_[f].as<float>() +
+                                         static_cast<size_t>(shot) * g.snapshots * m.grid_size()
+                                   : nullptr;
+    d.rec_cell = m.rec_cell_.as<int>();
+    d.rec_vx = c.nr ? raw_.as<float>() + raw_off_[k] : nullptr;
+    d.rec_vz = c.nr ? raw_.as<float>() + raw_off_[k] + static_cast<size_t>(c.nr) * nt_ : nullptr;
+    d.plan = m.plans_[shot];
+    d.stf = m.stf_d_.as<double>();
+    if (!tma::make_maps(d, m.mu_.as<float>(), tile_cfg_))
+      throw Error(PSV_ERR_CUDA, "tensor-map encoding failed for a batch member");
+    for (int cfg = 0; cfg < tma::kNumTileCfgs; ++cfg)
+      tma::append_tiles(cfg, static_cast<int>(k), g.nx, g.nz, tiles[cfg]);
+  }
+  descs_d_.allocate(descs.size() * sizeof(tma::SimDesc));
+  cuda_check(cudaMemcpy(descs_d_.get(), descs.data(), descs.size() * sizeof(tma::SimDesc),
+                        cudaMemcpyHostToDevice),
+             "upload batch descriptors");
+  for (int cfg = 0; cfg < tma::kNumTileCfgs; ++cfg) {
+    n_tiles_[cfg] = static_cast<int>(tiles[cfg].size());
+    tiles_d_[cfg].allocate(tiles[cfg].size() * sizeof(int4));
+    cuda_check(cudaMemcpy(tiles_d_[cfg].get(), tiles[cfg].data(), tiles[cfg].size() * sizeof(int4),
+                          cudaMemcpyHostToDevice),
+               "upload batch tiles");
+  }
+  built_ = true;
+}
+
+void Batch::set_tile_cfg(int cfg) {
+  if (cfg < 0 || cfg >= tma::kNumTileCfgs) throw Error(PSV_ERR_INVALID_ARGUMENT, "unknown tile shape");
+  if (cfg == tile_cfg_) return;
+  clear_graphs();
+  tile_cfg_ = cfg;
+  built_ = false;  // the descriptors' tensor maps depend on the tile shape
+}
+
+void Batch::synchronize() { cuda_check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize"); }
+
+void Batch::forward(bool store, int n_steps) {
+  if (members_.empty()) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+  struct Restore {
+    int dev;
+    ~Restore() { cudaSetDevice(dev); }
+  } restore{prev};
+  if (store) {
+    bool missing = false;
+    for (auto &mb : members_)
+      if (!mb.first->accu_[0].get()) {
+        mb.first->ensure_snapshots();
+        missing = true;
+      }
+    if (missing) {
+      built_ = false;
+      clear_graphs();
+    }
+  }
+  if (!built_) {
+    for (auto &mb : members_) mb.first->synchronize();
+    build();
+  }
+  const int steps = (n_steps <= 0 || n_steps > nt_) ? nt_ : n_steps;
+  const int cfg = tile_cfg_;
+  auto enqueue = [&]() {
+    cuda_check(cudaMemsetAsync(arena_.get(), 0, arena_.bytes(), stream_), "batch zero");
+    int parity = 0;
+    for (int it = 0; it < steps; ++it) {
+      cuda_check(tma::step(descs_d_.as<tma::SimDesc>(), tiles_d_[cfg].as<int4>(), n_tiles_[cfg],
+                           cfg, false, it, parity, store, err_flag_.as<int>(), stream_),
+                 "batch step");
+      parity ^= 1;
+    }
+    for (size_t k = 0; k < members_.size(); ++k) {
+      Model &m = *members_[k].first;
+      const Config &c = m.config();
+      if (!c.nr) continue;
+      const size_t off = static_cast<size_t>(members_[k].second) * c.nr * c.nt;
+      const float *raw = raw_.as<float>() + raw_off_[k];
+      cuda_check(receiver_cumsum_f32(c.nr, c.nt, steps, c.dt, c.dx * c.dz, raw,
+                                     raw + static_cast<size_t>(c.nr) * nt_,
+                                     m.rtf_[0].as<double>() + off, m.rtf_[1].as<double>() + off,
+                                     stream_),
+                 "batch seismograms");
+    }
+  };
+  if (graph_.exec && graph_.store == store && graph_.steps == steps) {
+    cuda_check(cudaGraphLaunch(graph_.exec, stream_), "cudaGraphLaunch");
+  } else if (graph_.uses == 0 || graph_.store != store || graph_.steps != steps) {
+    clear_graphs();
+    graph_.uses = 1;
+    graph_.store = store;
+    graph_.steps = steps;
+    enqueue();
+  } else {
+    cuda_check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal),
+               "cudaStreamBeginCapture");
+    try {
+      enqueue();
+    } catch (...) {
+      cudaGraph_t broken = nullptr;
+      cudaStreamEndCapture(stream_, &broken);
+      if (broken) cudaGraphDestroy(broken);
+      throw;
+    }
+    cudaGraph_t graph = nullptr;
+    cuda_check(cudaStreamEndCapture(stream_, &graph), "cudaStreamEndCapture");
+    cudaError_t e = cudaGraphInstantiate(&graph_.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    cuda_check(e, "cudaGraphInstantiate");
+    cuda_check(cudaGraphLaunch(graph_.exec, stream_), "cudaGraphLaunch");
+  }
+  synchronize();
+  int flag = 0;
+  cuda_check(cudaMemcpy(&flag, err_flag_.get(), sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+  if (flag) {
+    cudaMemset(err_flag_.get(), 0, sizeof(int));
+    throw Error(PSV_ERR_CUDA, "a CTA timed out waiting for its TMA tile copies");
+  }
+}
+
+int Batch::autotune(int n_steps) {
+  if (members_.empty()) return tile_cfg_;
+  float best = 0;
+  int best_cfg = tile_cfg_;
+  cudaEvent_t a, b;
+  cuda_check(cudaEventCreate(&a), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&b), "cudaEventCreate");
+  for (int cfg = 0; cfg < tma::kNumTileCfgs; ++cfg) {
+    set_tile_cfg(cfg);
+    forward(false, n_steps);  // eager run (also builds)
+    forward(false, n_steps);  // graph capture
+    cudaEventRecord(a, stream_);
+    forward(false, n_steps);
+    cudaEventRecord(b, stream_);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (cfg == 0 || ms < best) {
+      best = ms;
+      best_cfg = cfg;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  set_tile_cfg(best_cfg);
+  return best_cfg;
+}
+
+}  // namespace psv

@@ -1,0 +1,66 @@
+// Many simulations -- shots of many models, of uneven grid sizes -- advanced
+// together: one TMA-step launch per time step covers the tiles of every
+// simulation, and the whole time loop is replayed as one CUDA graph. No
+// counterpart in the reference, which runs one shot of one model at a time
+// (src/fdModel.cpp:1293-1296).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <utility>
+#include <vector>
+
+#include "psv_model.hpp"
+#include "psv_tma.hpp"
+
+namespace psv {
+
+class Batch {
+ public:
+  explicit Batch(int device);
+  ~Batch();
+  Batch(const Batch &) = delete;
+  Batch &operator=(const Batch &) = delete;
+
+  // Adds shot `shot` of `model` (FP32, TMA step). All models of a batch share
+  // nt. The models must outlive the batch.
+  void add(Model *model, int shot);
+  // Forward simulation of every member over its first n_steps time steps (all
+  // steps if n_steps <= 0). Seismograms land in each model's synthetic data of
+  // that shot; with store_fields, snapshots land in each model's snapshots.
+  void forward(bool store_fields, int n_steps);
+  // Times every tile shape on n_steps steps and keeps the fastest.
+  int autotune(int n_steps);
+  void set_tile_cfg(int cfg);
+  int tile_cfg() const { return tile_cfg_; }
+  int size() const { return static_cast<int>(members_.size()); }
+  double cells() const;  // grid points summed over members
+  int tiles() const { return n_tiles_[tile_cfg_]; }
+  void synchronize();
+
+ private:
+  void build();
+  void clear_graphs();
+
+  int device_;
+  cudaStream_t stream_ = nullptr;
+  std::vector<std::pair<Model *, int>> members_;
+  bool built_ = false;
+  int nt_ = 0;
+  int tile_cfg_ = tma::kTile16x28;
+  DeviceBuffer arena_;   // wave-field buffer sets of every member
+  DeviceBuffer raw_;     // receiver raw velocities of every member
+  DeviceBuffer descs_d_;
+  DeviceBuffer tiles_d_[tma::kNumTileCfgs];
+  int n_tiles_[tma::kNumTileCfgs] = {};
+  DeviceBuffer err_flag_;
+  std::vector<size_t> raw_off_;  // per member, floats into raw_
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    int uses = 0;
+    bool store = false;
+    int steps = 0;
+  } graph_;
+};
+
+}  // namespace psv

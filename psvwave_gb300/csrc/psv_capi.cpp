@@ -8,12 +8,18 @@
 #include <string>
 
 #include "../../include/psvwave.h"
+#include "psv_batch.hpp"
 #include "psv_model.hpp"
 
 struct psv_model {
   psv::Model impl;
   template <typename... A>
   explicit psv_model(A &&...a) : impl(std::forward<A>(a)...) {}
+};
+
+struct psv_batch {
+  psv::Batch impl;
+  explicit psv_batch(int device) : impl(device) {}
 };
 
 namespace {
@@ -509,6 +515,24 @@ const char *psv_step_kernel_name(const psv_model *m, int k) {
   return m->impl.step_kernel_name(k);
 }
 
+int psv_set_tile_shape(psv_model *m, int shape) {
+  return guarded([&] { M(m).set_tile_cfg(shape); });
+}
+
+int psv_get_tile_shape(const psv_model *m, int *shape) {
+  return guarded([&] {
+    need(shape, "shape");
+    *shape = M(m).tile_cfg();
+  });
+}
+
+int psv_autotune(psv_model *m, int n_steps, int *chosen) {
+  return guarded([&] {
+    const int c = M(m).autotune(n_steps > 0 ? n_steps : 50);
+    if (chosen) *chosen = c;
+  });
+}
+
 int psv_set_kernel_variant(psv_model *m, int variant) {
   return guarded([&] { M(m).set_variant(variant); });
 }
@@ -517,6 +541,78 @@ int psv_get_kernel_variant(const psv_model *m, int *variant) {
   return guarded([&] {
     need(variant, "variant");
     *variant = M(m).variant();
+  });
+}
+
+int psv_exact_gradient(psv_model *m, int checkpoint_every, double *misfit) {
+  return guarded([&] {
+    const double v = M(m).exact_gradient(checkpoint_every);
+    if (misfit) *misfit = v;
+  });
+}
+
+int psv_get_exact_gradient(psv_model *m, double *g_vp, double *g_vs, double *g_rho) {
+  return guarded([&] { M(m).get_exact_gradient(g_vp, g_vs, g_rho, false); });
+}
+
+int psv_get_exact_gradient_device(psv_model *m, double *g_vp, double *g_vs, double *g_rho) {
+  return guarded([&] { M(m).get_exact_gradient(g_vp, g_vs, g_rho, true); });
+}
+
+int psv_exact_bytes(const psv_model *m, int checkpoint_every, size_t *bytes) {
+  return guarded([&] {
+    need(bytes, "bytes");
+    *bytes = M(m).exact_bytes(checkpoint_every);
+  });
+}
+
+int psv_batch_create(int device, psv_batch **out) {
+  return guarded([&] {
+    need(out, "out");
+    *out = nullptr;
+    *out = new psv_batch(device);
+  });
+}
+
+int psv_batch_destroy(psv_batch *b) {
+  return guarded([&] { delete b; });
+}
+
+int psv_batch_add(psv_batch *b, psv_model *m, int i_shot) {
+  return guarded([&] {
+    need(b, "batch");
+    b->impl.add(&M(m), i_shot);
+  });
+}
+
+int psv_batch_forward(psv_batch *b, int store_fields, int n_steps) {
+  return guarded([&] {
+    need(b, "batch");
+    b->impl.forward(store_fields != 0, n_steps);
+  });
+}
+
+int psv_batch_set_tile_shape(psv_batch *b, int shape) {
+  return guarded([&] {
+    need(b, "batch");
+    b->impl.set_tile_cfg(shape);
+  });
+}
+
+int psv_batch_autotune(psv_batch *b, int n_steps, int *chosen) {
+  return guarded([&] {
+    need(b, "batch");
+    const int c = b->impl.autotune(n_steps > 0 ? n_steps : 50);
+    if (chosen) *chosen = c;
+  });
+}
+
+int psv_batch_info(const psv_batch *b, int *members, int *tiles, double *cells) {
+  return guarded([&] {
+    need(b, "batch");
+    if (members) *members = b->impl.size();
+    if (tiles) *tiles = b->impl.tiles();
+    if (cells) *cells = b->impl.cells();
   });
 }
 

@@ -91,8 +91,6 @@ Model::Model(const Config &cfg, int precision, int device)
   pitch_ = (geo_.nz + 3) / 4 * 4;
   build_tables();
   allocate();
-  build_tma_maps();
-  if (tma_ok_) variant_ = kFusedTma;
   // Homogeneous background medium (src/fdModel.cpp:249-261).
   std::vector<double> v(grid_size());
   const double scal[3] = {cfg_.scalar_vp, cfg_.scalar_vs, cfg_.scalar_rho};
@@ -105,6 +103,10 @@ Model::Model(const Config &cfg, int precision, int device)
   }
   update_from_velocity();
   build_plans();
+  // Large grids keep the 32 x 60 tiles; small ones fill the GPU with 16 x 28.
+  if (static_cast<double>(geo_.nx) * geo_.nz < 4.0e5) tile_cfg_ = tma::kTile16x28;
+  build_descs();
+  if (tma_ok_) variant_ = kFusedTma;
   synchronize();
 }
 
@@ -113,9 +115,9 @@ Model::Model(const Model &o)
       misfit_(o.misfit_), pitch_(o.pitch_), variant_(o.variant_), cur_(o.cur_) {
   DeviceGuard guard(device_);
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  tile_cfg_ = o.tile_cfg_;
   build_tables();
   allocate();
-  build_tma_maps();
   build_plans();
   const_cast<Model &>(o).synchronize();
   auto copy = [&](DeviceBuffer &d, const DeviceBuffer &s) {
@@ -143,6 +145,7 @@ Model::Model(const Model &o)
     copy(klame_[k], o.klame_[k]);
     copy(kvel_[k], o.kvel_[k]);
   }
+  build_descs();
 }
 
 Model::~Model() {
@@ -330,18 +333,295 @@ void Model::build_plans() {
   }
 }
 
-void Model::build_tma_maps() {
+void Model::build_descs() {
   tma_ok_ = false;
   if (prec_ != PSV_FP32 || !tma::supported(geo_.nx, geo_.nz, pitch_)) return;
-  const float *a[5], *b[5];
-  for (int f = 0; f < 5; ++f) {
-    a[f] = fields_[f].as<float>();
-    b[f] = fields2_[f].as<float>();
+  const int n_shots = cfg_.n_shots;
+  const size_t gsz = grid_size();
+  std::vector<tma::SimDesc> descs(static_cast<size_t>(2 * std::max(n_shots, 1)));
+  for (int k = 0; k < 2 * n_shots; ++k) {
+    const bool adjoint = k >= n_shots;
+    const int shot = adjoint ? k - n_shots : k;
+    tma::SimDesc &d = descs[k];
+    d.set[0] = fast::Fields{fields_[0].as<float>(), fields_[1].as<float>(), fields_[2].as<float>(),
+                            fields_[3].as<float>(), fields_[4].as<float>()};
+    d.set[1] = fast::Fields{fields2_[0].as<float>(), fields2_[1].as<float>(),
+                            fields2_[2].as<float>(), fields2_[3].as<float>(),
+                            fields2_[4].as<float>()};
+    d.nx = geo_.nx;
+    d.nz = geo_.nz;
+    d.pitch = pitch_;
+    d.np = cfg_.np_boundary;
+    d.nt = cfg_.nt;
+    d.nr = cfg_.nr;
+    d.si = cfg_.snapshot_interval;
+    d.dt = static_cast<float>(cfg_.dt);
+    d.idx = static_cast<float>(1.0 / cfg_.dx);
+    d.idz = static_cast<float>(1.0 / cfg_.dz);
+    d.dt_d = cfg_.dt;
+    d.lm = lm_.as<float>();
+    d.b = b_.as<float>();
+    d.taper_tab = taper_tab_d_.as<float>();
+    for (int f = 0; f < 5; ++f)
+      d.accu[f] = accu_[f].get()
+                      ? accu_[f].as<float>() + static_cast<size_t>(shot) * geo_.snapshots * gsz
+                      : nullptr;
+    d.krho = klame_[2].as<double>();
+    d.klam = klame_[0].as<double>();
+    d.kmu = klame_[1].as<double>();
+    d.sidt = cfg_.snapshot_interval * cfg_.dt;
+    d.fx0 = geo_.fx0;
+    d.fx1 = geo_.fx1;
+    d.fz0 = geo_.fz0;
+    d.fz1 = geo_.fz1;
+    d.rec_cell = rec_cell_.as<int>();
+    d.rec_vx = cfg_.nr ? rec_raw_.as<float>() : nullptr;
+    d.rec_vz = cfg_.nr ? rec_raw_.as<float>() + static_cast<size_t>(cfg_.nr) * cfg_.nt : nullptr;
+    if (!adjoint) {
+      d.plan = plans_[shot];
+      d.stf = stf_d_.as<double>();
+    } else {
+      d.plan = plans_[n_shots];
+      d.a_ux = a_stf_[0].as<double>() + static_cast<size_t>(shot) * cfg_.nr * cfg_.nt;
+      d.a_uz = a_stf_[1].as<double>() + static_cast<size_t>(shot) * cfg_.nr * cfg_.nt;
+    }
+    if (!tma::make_maps(d, mu_.as<float>(), tile_cfg_)) return;
   }
-  tma_ok_ = tma::make_maps(maps_[0], a, lm_.as<float>(), mu_.as<float>(), geo_.nx, geo_.nz,
-                           pitch_) &&
-            tma::make_maps(maps_[1], b, lm_.as<float>(), mu_.as<float>(), geo_.nx, geo_.nz,
-                           pitch_);
+  descs_h_ = std::move(descs);
+  tma_ok_ = true;
+}
+
+cudaError_t Model::tma_forward(int shot, bool store, int it0, int it1, bool zero, bool finish,
+                               cudaEvent_t *events) {
+  cudaStream_t s = stream();
+  if (zero) {
+    const size_t bytes = padded_size() * sizeof(float);
+    for (int f = 0; f < 5; ++f) {
+      cudaError_t e = cudaMemsetAsync(fields_[f].get(), 0, bytes, s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(fields2_[f].get(), 0, bytes, s);
+      if (e != cudaSuccess) return e;
+    }
+    cur_ = 0;
+  }
+  const tma::SimDesc &h = descs_h_[shot];
+  const int cfg = tile_cfg_;
+  for (int it = it0; it < it1; ++it) {
+    cudaEvent_t *ev = events ? events + 2 * (it - it0) : nullptr;
+    if (ev) cudaEventRecord(ev[0], s);
+    cudaError_t e = tma::step_single(h, cfg, false, it, cur_, store, err_flag_.as<int>(), s);
+    if (ev) cudaEventRecord(ev[1], s);
+    if (e != cudaSuccess) return e;
+    cur_ ^= 1;
+  }
+  if (finish && cfg_.nr) {
+    const size_t off = static_cast<size_t>(shot) * cfg_.nr * cfg_.nt;
+    const float *raw = rec_raw_.as<float>();
+    cudaError_t e = receiver_cumsum_f32(cfg_.nr, cfg_.nt, it1, cfg_.dt, cfg_.dx * cfg_.dz, raw,
+                                        raw + static_cast<size_t>(cfg_.nr) * cfg_.nt,
+                                        rtf_[0].as<double>() + off, rtf_[1].as<double>() + off, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t Model::tma_adjoint(int shot) {
+  cudaStream_t s = stream();
+  const size_t bytes = padded_size() * sizeof(float);
+  for (int f = 0; f < 5; ++f) {
+    cudaError_t e = cudaMemsetAsync(fields_[f].get(), 0, bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(fields2_[f].get(), 0, bytes, s);
+    if (e != cudaSuccess) return e;
+  }
+  cur_ = 0;
+  const tma::SimDesc &h = descs_h_[cfg_.n_shots + shot];
+  const int cfg = tile_cfg_;
+  for (int it = cfg_.nt - 1; it >= 0; --it) {
+    cudaError_t e = tma::step_single(h, cfg, true, it, cur_, false, err_flag_.as<int>(), s);
+    if (e != cudaSuccess) return e;
+    cur_ ^= 1;
+  }
+  return cudaGetLastError();
+}
+
+size_t Model::exact_bytes(int C) const {
+  const int nt = cfg_.nt;
+  if (C <= 0 || C > nt) C = nt;
+  const size_t state = 5 * padded_size() * elem();
+  const size_t n_ck = (nt + C - 1) / C;
+  return n_ck * state + (C + 1) * state + 8 * padded_size() * elem() +
+         7 * grid_size() * sizeof(double);
+}
+
+double Model::exact_gradient(int C) {
+  DeviceGuard guard(device_);
+  const int nt = cfg_.nt, n_shots = cfg_.n_shots, nr = cfg_.nr;
+  if (C <= 0 || C > nt) C = nt;
+  const int n_ck = (nt + C - 1) / C;
+  const size_t gp = padded_size(), g = grid_size(), e = elem();
+  const size_t state_elems = 5 * gp;
+  cudaStream_t s = stream();
+  auto ensure = [&](DeviceBuffer &b, size_t bytes) {
+    if (b.bytes() < bytes) b.allocate(bytes);
+  };
+  for (auto &b : gex_) ensure(b, g * sizeof(double));
+  for (auto &b : kexact_) ensure(b, g * sizeof(double));
+  for (auto &b : adj_) ensure(b, data_size() * sizeof(double));
+  for (auto &b : lam_) ensure(b, gp * e);
+  ensure(ckpt_, n_ck * state_elems * e);
+  ensure(slots_, (C + 1) * state_elems * e);
+  for (auto &b : gex_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "exact zero");
+
+  SolverArgs a = solver_args();
+  unsigned char *ck = ckpt_.as<unsigned char>(), *sl = slots_.as<unsigned char>();
+  auto save_state = [&](unsigned char *dst) {
+    for (int f = 0; f < 5; ++f)
+      cuda_check(cudaMemcpyAsync(dst + f * gp * e, fields_[f].get(), gp * e,
+                                 cudaMemcpyDeviceToDevice, s),
+                 "save state");
+  };
+  auto load_state = [&](const unsigned char *src) {
+    for (int f = 0; f < 5; ++f)
+      cuda_check(cudaMemcpyAsync(fields_[f].get(), src + f * gp * e, gp * e,
+                                 cudaMemcpyDeviceToDevice, s),
+                 "load state");
+  };
+  auto fwd = [&](int shot, int it0, int it1, bool finish) {
+    cudaError_t err = prec_ == PSV_FP64
+                          ? forward_f64(a, plans_[shot], shot, false, it0, it1, false, finish, s)
+                          : forward_f32(a, plans_[shot], shot, false, it0, it1, false, finish, s);
+    cuda_check(err, "exact forward");
+  };
+  cur_ = 0;
+  // 1. Forward runs of every shot for the seismograms (and misfit).
+  for (int shot = 0; shot < n_shots; ++shot) {
+    for (auto &f : fields_) cuda_check(cudaMemsetAsync(f.get(), 0, f.bytes(), s), "zero");
+    fwd(shot, 0, nt, true);
+  }
+  const double misfit = calculate_l2_misfit();
+  // 2. Receiver terms of the adjoint.
+  for (int c = 0; c < 2; ++c)
+    cuda_check(exact_receiver_terms(n_shots * nr, nt, cfg_.dt, cfg_.dx * cfg_.dz,
+                                    rtf_[c].as<double>(), rtf_true_[c].as<double>(),
+                                    adj_[c].as<double>(), s),
+               "receiver terms");
+  // 3. Per shot: checkpointed forward, then segments backwards.
+  for (int shot = 0; shot < n_shots; ++shot) {
+    for (auto &f : fields_) cuda_check(cudaMemsetAsync(f.get(), 0, f.bytes(), s), "zero");
+    for (int k = 0; k < n_ck; ++k) {
+      save_state(ck + k * state_elems * e);
+      if (k + 1 < n_ck) fwd(shot, k * C, (k + 1) * C, false);
+    }
+    for (auto &b : lam_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "zero adjoint");
+    void *lt[3] = {lam_[2].get(), lam_[3].get(), lam_[4].get()};
+    void *ot[3] = {lam_[5].get(), lam_[6].get(), lam_[7].get()};
+    for (int k = n_ck - 1; k >= 0; --k) {
+      const int s0 = k * C, s1 = std::min(nt, s0 + C);
+      load_state(ck + k * state_elems * e);
+      save_state(sl);
+      for (int n = s0; n < s1; ++n) {
+        fwd(shot, n, n + 1, false);
+        save_state(sl + (n + 1 - s0) * state_elems * e);
+      }
+      for (int n = s1 - 1; n >= s0; --n) {
+        ExactStepArgs x;
+        x.nx = geo_.nx;
+        x.nz = geo_.nz;
+        x.pitch = pitch_;
+        x.np = cfg_.np_boundary;
+        x.nt = nt;
+        x.it = n;
+        x.nr = nr;
+        x.dt = cfg_.dt;
+        x.dx = cfg_.dx;
+        x.dz = cfg_.dz;
+        x.lm = lm_.get();
+        x.la = la_.get();
+        x.mu = mu_.get();
+        x.b = b_.get();
+        x.taper_tab = taper_tab_d_.get();
+        x.lv[0] = lam_[0].get();
+        x.lv[1] = lam_[1].get();
+        for (int f = 0; f < 3; ++f) {
+          x.lt[f] = lt[f];
+          x.ot[f] = ot[f];
+        }
+        const unsigned char *sv = sl + (n - s0) * state_elems * e;      // v^n
+        const unsigned char *st = sl + (n + 1 - s0) * state_elems * e;  // tau^(n+1)
+        x.fv[0] = sv;
+        x.fv[1] = sv + gp * e;
+        x.ft[0] = st + 2 * gp * e;
+        x.ft[1] = st + 3 * gp * e;
+        x.ft[2] = st + 4 * gp * e;
+        x.g_lm = gex_[0].as<double>();
+        x.g_la = gex_[1].as<double>();
+        x.g_mu = gex_[2].as<double>();
+        x.g_b = gex_[3].as<double>();
+        x.plan = plans_[shot];
+        x.stf = stf_d_.as<double>();
+        x.rec_cell = rec_cell_.as<int>();
+        x.adj_x = adj_[0].as<double>() + static_cast<size_t>(shot) * nr * nt;
+        x.adj_z = adj_[1].as<double>() + static_cast<size_t>(shot) * nr * nt;
+        cuda_check(prec_ == PSV_FP64 ? exact_step_f64(x, s) : exact_step_f32(x, s), "exact step");
+        std::swap(lt[0], ot[0]);
+        std::swap(lt[1], ot[1]);
+        std::swap(lt[2], ot[2]);
+      }
+    }
+  }
+  // 4. Chain rule to (vp, vs, rho).
+  cuda_check(exact_chain(g, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(),
+                         gex_[0].as<double>(), gex_[1].as<double>(), gex_[2].as<double>(),
+                         gex_[3].as<double>(), kexact_[0].as<double>(), kexact_[1].as<double>(),
+                         kexact_[2].as<double>(), s),
+             "exact chain");
+  synchronize();
+  return misfit;
+}
+
+void Model::get_exact_gradient(double *g_vp, double *g_vs, double *g_rho, bool device_pointers) {
+  DeviceGuard guard(device_);
+  if (!kexact_[0].get()) throw Error(PSV_ERR_INVALID_ARGUMENT, "no exact gradient computed yet");
+  const size_t bytes = grid_size() * sizeof(double);
+  double *out[3] = {g_vp, g_vs, g_rho};
+  for (int k = 0; k < 3; ++k)
+    if (out[k])
+      cuda_check(cudaMemcpyAsync(out[k], kexact_[k].get(), bytes,
+                                 device_pointers ? cudaMemcpyDeviceToDevice
+                                                 : cudaMemcpyDeviceToHost,
+                                 stream()),
+                 "get_exact_gradient");
+  synchronize();
+}
+
+void Model::set_tile_cfg(int cfg) {
+  if (cfg < 0 || cfg >= tma::kNumTileCfgs) throw Error(PSV_ERR_INVALID_ARGUMENT, "unknown tile shape");
+  if (cfg == tile_cfg_) return;
+  DeviceGuard guard(device_);
+  clear_graphs();
+  tile_cfg_ = cfg;
+  if (tma_ok_) {
+    synchronize();
+    build_descs();
+  }
+}
+
+int Model::autotune(int n_steps) {
+  if (!(prec_ == PSV_FP32 && variant_ == kFusedTma)) return tile_cfg_;
+  if (cfg_.n_shots < 1) return tile_cfg_;
+  double best = 0;
+  int best_cfg = tile_cfg_;
+  for (int c = 0; c < tma::kNumTileCfgs; ++c) {
+    set_tile_cfg(c);
+    double per_step = 0;
+    profile_forward(0, std::min(n_steps, cfg_.nt), &per_step, nullptr, 0);  // warm
+    profile_forward(0, std::min(n_steps, cfg_.nt), &per_step, nullptr, 0);
+    if (c == 0 || per_step < best) {
+      best = per_step;
+      best_cfg = c;
+    }
+  }
+  set_tile_cfg(best_cfg);
+  return best_cfg;
 }
 
 void Model::check_device_error() {
@@ -400,7 +680,9 @@ void Model::run_loop(int direction, int shot, bool store, int n_steps,
 void Model::ensure_snapshots() {
   if (accu_[0].get()) return;
   const size_t n = static_cast<size_t>(cfg_.n_shots) * geo_.snapshots * grid_size();
+  synchronize();
   for (auto &a : accu_) a.allocate(n * elem());
+  if (tma_ok_) build_descs();
 }
 
 size_t Model::device_bytes() const {
@@ -504,8 +786,7 @@ void Model::forward_simulate(int shot, bool store, bool verbose, bool output_wav
     if (prec_ == PSV_FP64)
       e = forward_f64(a, plan, shot, store, it0, it1, zero, fin, stream());
     else if (variant_ == kFusedTma)
-      e = tma::forward(a, second, &cur_, maps_, err_flag_.as<int>(), plan, shot, store, it0, it1,
-                       zero, fin, stream());
+      e = tma_forward(shot, store, it0, it1, zero, fin, nullptr);
     else if (variant_ == kFused)
       e = fast::forward(a, second, &cur_, plan, shot, store, it0, it1, zero, fin, stream());
     else
@@ -551,8 +832,7 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
   if (prec_ == PSV_FP64)
     err = forward_f64(a, plans_[shot], shot, false, 0, n_steps, true, false, stream());
   else if (variant_ == kFusedTma)
-    err = tma::forward(a, second, &cur_, maps_, err_flag_.as<int>(), plans_[shot], shot, false, 0,
-                       n_steps, true, false, stream());
+    err = tma_forward(shot, false, 0, n_steps, true, false, a.events);
   else if (variant_ == kFused)
     err = fast::forward(a, second, &cur_, plans_[shot], shot, false, 0, n_steps, true, false,
                         stream());
@@ -623,8 +903,7 @@ void Model::adjoint_simulate(int shot, bool verbose) {
       e = adjoint_f64(a, plans_[cfg_.n_shots], shot, stream());
       cur_ = 0;
     } else if (variant_ == kFusedTma) {
-      e = tma::adjoint(a, second, &cur_, maps_, err_flag_.as<int>(), plans_[cfg_.n_shots], shot,
-                       stream());
+      e = tma_adjoint(shot);
     } else if (variant_ == kFused) {
       e = fast::adjoint(a, second, &cur_, plans_[cfg_.n_shots], shot, stream());
     } else {

@@ -56,7 +56,11 @@ class DeviceBuffer {
 // Throws Error(PSV_ERR_CUDA) when e is not cudaSuccess.
 void cuda_check(cudaError_t e, const char *what);
 
+class Batch;
+
 class Model {
+  friend class Batch;
+
  public:
   Model(const Config &cfg, int precision, int device);
   Model(const Model &other);  // deep copy (src/fdModel.cpp:64-97)
@@ -118,6 +122,20 @@ class Model {
   // Time-step kernel variant (Variant in psv_solver.hpp); FP64 models only
   // run kTwoKernel.
   void set_variant(int v);
+  // Tile shape of the TMA step (tma::TileCfg); autotune() times each shape
+  // on a few forward steps of shot 0 and keeps the fastest.
+  void set_tile_cfg(int cfg);
+  int tile_cfg() const { return tile_cfg_; }
+  int autotune(int n_steps);
+
+  // Gradient of the L2 misfit over all shots with respect to (vp, vs, rho)
+  // by the exact discrete adjoint (psv_exact.cuh), with the forward states
+  // rebuilt from checkpoints taken every `checkpoint_every` steps (>= nt:
+  // one segment, every state kept). Returns the misfit; the gradient stays on
+  // the device (get_exact_gradient).
+  double exact_gradient(int checkpoint_every);
+  void get_exact_gradient(double *g_vp, double *g_vs, double *g_rho, bool device_pointers);
+  size_t exact_bytes(int checkpoint_every) const;
   int variant() const { return variant_; }
   int kernels_per_step() const { return variant_ == kTwoKernel ? 2 : 1; }
   const char *step_kernel_name(int k) const;
@@ -167,9 +185,16 @@ class Model {
   int pitch_ = 0;
   int variant_ = kTwoKernel;
   int cur_ = 0;  // fused variants: 0 = fields_ hold the current state, 1 = fields2_
-  bool tma_ok_ = false;   // TMA maps built for this model
-  tma::Maps maps_[2];     // tensor maps of fields_ (0) and fields2_ (1) + medium
-  void build_tma_maps();
+  // TMA step: one simulation descriptor per (direction, shot) --
+  // [0, n_shots) forward, [n_shots, 2 n_shots) adjoint -- on the host (their
+  // tensor maps go out as kernel parameters) and in device memory.
+  bool tma_ok_ = false;
+  int tile_cfg_ = tma::kTile32x60;
+  std::vector<tma::SimDesc> descs_h_;
+  void build_descs();
+  cudaError_t tma_forward(int shot, bool store, int it0, int it1, bool zero, bool finish,
+                          cudaEvent_t *events);
+  cudaError_t tma_adjoint(int shot);
   void check_device_error();
 
   // Whole time loops captured as CUDA graphs, keyed by (direction, shot,
@@ -202,6 +227,9 @@ class Model {
   DeviceBuffer kvel_[3];                      // vp vs rho           (FP64)
   DeviceBuffer partials_, scalar_;            // reduction scratch   (FP64)
   DeviceBuffer err_flag_;                     // int, raised by bounded device waits
+  // exact adjoint: FP64 gradients wrt (lm, la, mu, b) and (vp, vs, rho),
+  // receiver terms, adjoint state (lv x2, lt x3, ot x3), checkpoints, slots
+  DeviceBuffer gex_[4], kexact_[3], adj_[2], lam_[8], ckpt_, slots_;
   // Injection plans: one per shot (sources) and one for the adjoint receivers.
   std::vector<DeviceBuffer> plan_terms_, plan_maps_;
   std::vector<InjPlan> plans_;  // [n_shots] forward, [n_shots] = adjoint

@@ -93,6 +93,29 @@ PSV_SOLVER_DECLS(f32)
 PSV_SOLVER_DECLS(f64)
 #undef PSV_SOLVER_DECLS
 
+// One step of the exact discrete adjoint (psv_exact.cuh): from the adjoint
+// state after step `it` to the state before it, accumulating the FP64 medium
+// gradients. lv (vx, vz) and lt (txx, tzz, txz) are updated in place, the
+// new stress adjoint goes to ot; fv holds v^it and ft tau^(it+1) of the
+// forward run. Arrays are padded [nx][pitch] of the wave-field precision.
+struct ExactStepArgs {
+  int nx = 0, nz = 0, pitch = 0, np = 0, nt = 0, it = 0, nr = 0;
+  double dt = 0, dx = 0, dz = 0;
+  const void *lm = nullptr, *la = nullptr, *mu = nullptr, *b = nullptr, *taper_tab = nullptr;
+  void *lv[2] = {nullptr, nullptr};
+  void *lt[3] = {nullptr, nullptr, nullptr};
+  void *ot[3] = {nullptr, nullptr, nullptr};
+  const void *fv[2] = {nullptr, nullptr};
+  const void *ft[3] = {nullptr, nullptr, nullptr};
+  double *g_lm = nullptr, *g_la = nullptr, *g_mu = nullptr, *g_b = nullptr;
+  InjPlan plan{};
+  const double *stf = nullptr;
+  const int *rec_cell = nullptr;           // padded receiver cells
+  const double *adj_x = nullptr, *adj_z = nullptr;  // receiver terms [nr][nt] of the shot
+};
+cudaError_t exact_step_f32(const ExactStepArgs &e, cudaStream_t s);
+cudaError_t exact_step_f64(const ExactStepArgs &e, cudaStream_t s);
+
 // Seismograms from raw FP32 receiver velocities (psv_solver_f32.cu).
 cudaError_t receiver_cumsum_f32(int nr, int nt, int n_steps, double dt, double dxdz,
                                 const float *raw_x, const float *raw_z, double *out_x,
@@ -108,5 +131,16 @@ cudaError_t adjoint_sources_l2(size_t n, const double *syn_ux, const double *obs
 cudaError_t map_kernels(size_t n, const double *vp, const double *vs, const double *rho,
                         const double *k_lam, const double *k_mu, const double *k_rho,
                         double *vp_k, double *vs_k, double *rho_k, cudaStream_t s);
+// Receiver terms of the exact adjoint: adj[r][n] = dt / (dx dz) *
+// sum_{m >= n} dt (syn[r][m] - obs[r][m]), per receiver row of length nt.
+cudaError_t exact_receiver_terms(int rows, int nt, double dt, double dxdz, const double *syn,
+                                 const double *obs, double *adj, cudaStream_t s);
+// Gradients with respect to (vp, vs, rho) from those with respect to
+// (lm, la, mu, b): lm = rho vp^2, la = rho (vp^2 - 2 vs^2), mu = rho vs^2,
+// b = 1 / rho.
+cudaError_t exact_chain(size_t n, const double *vp, const double *vs, const double *rho,
+                        const double *g_lm, const double *g_la, const double *g_mu,
+                        const double *g_b, double *g_vp, double *g_vs, double *g_rho,
+                        cudaStream_t s);
 
 }  // namespace psv

@@ -1,8 +1,10 @@
 // Single-precision wave fields: the production path. Seismograms, misfit and
 // kernel sums stay FP64.
+#include "psv_exact.cuh"
 #include "psv_kernels.cuh"
 
 PSV_DEFINE_SOLVER(float, f32)
+PSV_DEFINE_EXACT(float, f32)
 
 namespace psv {
 cudaError_t receiver_cumsum_f32(int nr, int nt, int n_steps, double dt, double dxdz,

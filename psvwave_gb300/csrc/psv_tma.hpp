@@ -1,9 +1,19 @@
-// FP32 fused time step with TMA tile loads (psv_tma_f32.cu).
+// FP32 fused time step with TMA tile loads (psv_tma_f32.cu), for one or many
+// simulations per launch.
+//
+// A *simulation* is one shot of one model: its wave-field buffer sets, its
+// medium, receivers, injection terms and (per shot) snapshot block. Every
+// launch advances every simulation of a table by one time step; the CTAs of
+// the launch are the tiles of all simulations, listed in a tile table. A
+// single model's shot is a table of one.
 #pragma once
 
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <vector>
+
+#include "psv_fast.hpp"
 #include "psv_solver.hpp"
 
 namespace psv {
@@ -14,23 +24,51 @@ struct Maps {
   CUtensorMap vx, vz, txx, tzz, txz, lm, mu;
 };
 
-// True when the arrays can use the TMA kernel (row pitch a multiple of 4
-// points, i.e. rows on 16-byte boundaries) and the driver exposes
-// tensor-map encoding.
+// Tile shapes (x rows by z columns, threads per CTA).
+enum TileCfg { kTile32x60 = 0, kTile16x28 = 1, kNumTileCfgs = 2 };
+void tile_dims(int cfg, int *tx, int *tz);
+
+// Everything a CTA needs about its simulation; lives in device memory.
+struct alignas(128) SimDesc {
+  Maps maps[2];                // tensor maps for the descriptor's tile shape; parity p reads set p
+  fast::Fields set[2];         // wave-field buffer sets
+  int nx = 0, nz = 0, pitch = 0, np = 0, nt = 0, nr = 0, si = 1;
+  float dt = 0, idx = 0, idz = 0;
+  double dt_d = 0;
+  const float *lm = nullptr, *b = nullptr, *taper_tab = nullptr;
+  float *accu[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // this shot's snapshots
+  double *krho = nullptr, *klam = nullptr, *kmu = nullptr;
+  double sidt = 0;
+  int fx0 = 0, fx1 = 0, fz0 = 0, fz1 = 0;
+  const int *rec_cell = nullptr;  // padded cells
+  float *rec_vx = nullptr, *rec_vz = nullptr;  // [nr][nt]
+  InjPlan plan{};                 // forward: sources of the shot; adjoint: receivers
+  const double *stf = nullptr, *a_ux = nullptr, *a_uz = nullptr;
+};
+
+// True when tensor-map encoding is available and the row pitch is a
+// multiple of 4 points (16-byte rows).
 bool supported(int nx, int nz, int pitch);
 
-// Encodes the maps of one buffer set; false on failure.
-bool make_maps(Maps &m, const float *const fields[5], const float *lm, const float *mu, int nx,
-               int nz, int pitch);
+// Encodes desc.maps for tile shape `cfg` from desc.set, desc.lm and the mu
+// array; false on failure.
+bool make_maps(SimDesc &desc, const float *mu, int cfg);
 
-// Time loops as fast::forward / fast::adjoint; maps[0] covers the primary
-// buffer set, maps[1] the second. *err (device int) is raised when a CTA's
-// bounded wait for its copies times out.
-cudaError_t forward(const SolverArgs &a, void *const second[5], int *cur, const Maps maps[2],
-                    int *err, const InjPlan &plan, int shot, bool store, int it0, int it1,
-                    bool zero_first, bool finish, cudaStream_t s);
-cudaError_t adjoint(const SolverArgs &a, void *const second[5], int *cur, const Maps maps[2],
-                    int *err, const InjPlan &plan, int shot, cudaStream_t s);
+// Appends the tiles of simulation `sim` (one int4 per CTA: sim, x0, z0,
+// first-tile flag) for tile shape `cfg`.
+void append_tiles(int cfg, int sim, int nx, int nz, std::vector<int4> &tiles);
+
+// One time step of every simulation in `sims` (device table), over the
+// tiles in `tiles` (device, n_tiles entries). parity p: inputs in set p,
+// outputs in set 1 - p. store: forward snapshots at steps it % si == 0.
+// *err is raised when a CTA's bounded wait for its copies times out.
+cudaError_t step(const SimDesc *sims, const int4 *tiles, int n_tiles, int cfg, bool adjoint,
+                 int it, int parity, bool store, int *err, cudaStream_t s);
+
+// The same step for one simulation whose descriptor `desc` goes out whole
+// as a kernel parameter; tiles follow from the grid.
+cudaError_t step_single(const SimDesc &desc, int cfg, bool adjoint, int it, int parity,
+                        bool store, int *err, cudaStream_t s);
 
 }  // namespace tma
 }  // namespace psv

@@ -234,6 +234,23 @@ class fdModel:
         self.run_model(verbose=verbose, simulate_adjoint=True)
         return self.misfit, self.get_gradient_vector()
 
+    def exact_gradient(self, checkpoint_every=100):
+        """Misfit and its gradient with respect to (vp, vs, rho) over all
+        shots by the exact discrete adjoint (the transpose of the time
+        stepping), with forward states rebuilt from checkpoints every
+        `checkpoint_every` steps. Returns (misfit, (g_vp, g_vs, g_rho))."""
+        mis = ctypes.c_double()
+        _capi.check(self._lib.psv_exact_gradient(self._h, int(checkpoint_every), ctypes.byref(mis)))
+        g = [_out((self.nx, self.nz)) for _ in range(3)]
+        _capi.check(self._lib.psv_get_exact_gradient(self._h, *[_ptr(a) for a in g]))
+        self._info.misfit = mis.value
+        return mis.value, tuple(g)
+
+    def exact_bytes(self, checkpoint_every=100):
+        n = ctypes.c_size_t()
+        _capi.check(self._lib.psv_exact_bytes(self._h, int(checkpoint_every), ctypes.byref(n)))
+        return n.value
+
     def update_from_velocity(self):
         _capi.check(self._lib.psv_update_from_velocity(self._h))
 
@@ -428,3 +445,22 @@ class fdModel:
     @kernel_variant.setter
     def kernel_variant(self, name):
         _capi.check(self._lib.psv_set_kernel_variant(self._h, self.VARIANTS[name]))
+
+    TILE_SHAPES = {"32x60": 0, "16x28": 1}
+
+    @property
+    def tile_shape(self):
+        """Tile shape (x rows by z columns) of the FP32 TMA step."""
+        v = ctypes.c_int()
+        _capi.check(self._lib.psv_get_tile_shape(self._h, ctypes.byref(v)))
+        return {0: "32x60", 1: "16x28"}[v.value]
+
+    @tile_shape.setter
+    def tile_shape(self, name):
+        _capi.check(self._lib.psv_set_tile_shape(self._h, self.TILE_SHAPES[name]))
+
+    def autotune(self, n_steps=50):
+        """Time every tile shape on n_steps forward steps; keep the fastest."""
+        v = ctypes.c_int()
+        _capi.check(self._lib.psv_autotune(self._h, int(n_steps), ctypes.byref(v)))
+        return {0: "32x60", 1: "16x28"}[v.value]

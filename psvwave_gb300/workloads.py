@@ -84,3 +84,35 @@ def c1_media(seed=1):
     p = c1_params()
     nx, nz = p["nx_inner"] + 2 * p["np_boundary"], p["nz_inner"] + 2 * p["np_boundary"]
     return layered_media(nx, nz, p["np_boundary"], 30, seed)
+
+
+def c2_models(n_models=256, nt=1000, seed=2):
+    """The batching workload: n_models independent models of uneven sizes,
+    nx_inner uniform in [200, 800] and nz_inner in [100, 400], each with a
+    25-cell boundary and 1-4 shots (one source per shot, evenly spaced at
+    z = 10), Ricker 20-50 Hz, 50 receivers along z = 5, seeded layered +
+    Gaussian-random media as c1. dx = dz = 5, dt = 4e-4, and nt = 1000
+    steps (the configuration leaves nt open). Returns [(params, media)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_models):
+        nxi = int(rng.integers(200, 801))
+        nzi = int(rng.integers(100, 401))
+        shots = int(rng.integers(1, 5))
+        nb = 25
+        xs = [int(nxi * (s + 1) / (shots + 1)) for s in range(shots)]
+        nr = 50
+        p = dict(nt=nt, nx_inner=nxi, nz_inner=nzi, nx_inner_boundary=10, nz_inner_boundary=10,
+                 dx=5.0, dz=5.0, dt=4e-4, np_boundary=nb, np_factor=0.015,
+                 scalar_rho=2000.0, scalar_vp=2500.0, scalar_vs=1445.0, npx=1, npz=1,
+                 peak_frequency=float(rng.uniform(20.0, 50.0)), source_timeshift=0.0,
+                 delay_cycles_per_shot=0, n_sources=shots, ix_sources=xs,
+                 iz_sources=[10] * shots,
+                 moment_angles=[float(a) for a in rng.uniform(0.0, 180.0, shots)],
+                 which_source_to_fire_in_which_shot=[[s] for s in range(shots)], nr=nr,
+                 ix_receivers=[int(2 + (nxi - 4) * r / (nr - 1)) for r in range(nr)],
+                 iz_receivers=[5] * nr, snapshot_interval=nt)
+        media = layered_media(nxi + 2 * nb, nzi + 2 * nb, nb, 30, seed=1000 * seed + k,
+                              corr_len=20.0)
+        out.append((p, media))
+    return out

@@ -216,3 +216,23 @@ def test_fp32_tma_vs_two_kernel_agree(golden):
         assert rel_l2(a, b) <= 1e-5
     for a, b in zip(res[0][1], res[1][1]):
         assert rel_l2(a, b) <= 1e-5
+
+
+def test_tile_shapes_agree_and_autotune(golden):
+    """Both tile shapes of the TMA step give the same seismograms to FP32
+    rounding and stay within tolerance of the reference; the autotuner picks
+    one of them."""
+    res = {}
+    for shape in ("32x60", "16x28"):
+        m = psv.fdModel(SMALL_INI, precision="fp32")
+        m.tile_shape = shape
+        assert m.tile_shape == shape
+        fwi_gradient(m, tuple(golden["target"]), tuple(golden["start"]))
+        out = gpu_outputs(m)
+        for name in OUTPUTS:
+            assert rel_l2(out[name], golden[name]) <= FP32_TOL, (shape, name)
+        res[shape] = out
+    for name in ("rtf_ux", "rtf_uz"):
+        assert rel_l2(res["32x60"][name], res["16x28"][name]) <= 1e-5
+    m = psv.fdModel(SMALL_INI, precision="fp32")
+    assert m.autotune(20) in ("32x60", "16x28")
