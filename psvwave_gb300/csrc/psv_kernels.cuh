@@ -367,9 +367,13 @@ cudaError_t run_forward(const SolverArgs &a, const InjPlan &plan, int shot, bool
   }
   if (finish && a.nr) {
     const size_t off = (size_t)shot * a.nr * a.nt;
-    kern::receiver_cumsum<T><<<(2 * a.nr + 127) / 128, 128, 0, s>>>(
-        a.nr, a.nt, it1, a.dt, a.dx * a.dz, e.rec_vx, e.rec_vz, a.rtf_ux + off,
-        a.rtf_uz + off);
+    if constexpr (sizeof(T) == 4)
+      return receiver_cumsum_f32(a.nr, a.nt, it1, a.dt, a.dx * a.dz, (const float *)e.rec_vx,
+                                 (const float *)e.rec_vz, a.rtf_ux + off, a.rtf_uz + off, s);
+    else
+      kern::receiver_cumsum<T><<<(2 * a.nr + 127) / 128, 128, 0, s>>>(
+          a.nr, a.nt, it1, a.dt, a.dx * a.dz, e.rec_vx, e.rec_vz, a.rtf_ux + off,
+          a.rtf_uz + off);
   }
   return cudaGetLastError();
 }

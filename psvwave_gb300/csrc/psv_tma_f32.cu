@@ -129,6 +129,31 @@ __device__ __forceinline__ void inject(const SimDesc &d, int it, int g, int gx, 
   }
 }
 
+// Programmatic dependent launch: a step launched with programmatic stream
+// serialisation may start while the previous step drains; griddep_wait
+// returns once that step has completed and its writes are visible (a no-op
+// for launches without the attribute).
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// An interior tile computes every stress point of its box (rows X0-2 ..
+// X0+TX+1, columns Z0-2 .. Z0+TZ+1) inside the updated region 2 <= x < n-2
+// and at least np frames deep (taper exactly 1), has no source or
+// adjoint-source term among its own points and no snapshot I/O this step.
+// Its copies then lie wholly inside the grid and it needs no per-point test.
+template <class S>
+__device__ __forceinline__ bool interior_tile(const SimDesc &d, int X0, int Z0, bool snap_io) {
+  const int lo = max(2, d.np - 1);
+  const InjPlan &p = d.plan;
+  const bool inj = p.n && X0 < p.x0 + p.w && p.x0 < X0 + S::TX && Z0 < p.z0 + p.h &&
+                   p.z0 < Z0 + S::TZ;
+  return !snap_io && !inj && X0 - 2 >= lo && Z0 - 2 >= lo &&
+         X0 + S::TX + 1 <= min(d.nx - 3, d.nx - d.np) &&
+         Z0 + S::TZ + 1 <= min(d.nz - 3, d.nz - d.np);
+}
+
 // One tile's time step. `maps` are the tensor maps of this step's input set;
 // the kernels below pass them either as a kernel parameter (single model:
 // the copies can be issued without waiting for any load) or from the
@@ -162,6 +187,28 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
+  // Snapshot step: forward stores the pre-step state, adjoint correlates
+  // with it (both at this shot's snapshot it / si).
+  const bool snap_io = (it % d.si) == 0 && d.accu[0] != nullptr && (ADJ || store);
+  const size_t soff = (size_t)(it / d.si) * nx * nz;
+  const bool inner = interior_tile<S>(d, X0, Z0, snap_io);
+
+  // This thread's buoyancy values for phase C (the medium does not change
+  // between steps, so they load before the previous step has finished).
+  // Interior tiles give each row group consecutive rows, the others every
+  // G-th row.
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = w % S::H, q = w / S::H;
+  constexpr int KC = TX / G;  // own rows per thread
+  const int lzc = h * 32 + lane;  // own column of this thread (valid if < TZ)
+  const int gzc = Z0 + lzc;
+  const bool col_ok = lzc < TZ && gzc < nz;
+  float bb[KC];
+#pragma unroll
+  for (int k = 0; k < KC; ++k) {
+    const int gx = inner ? X0 + q * KC + k : X0 + q + G * k;
+    bb[k] = (col_ok && gx < nx) ? __ldg(d.b + gx * ps + gzc) : 0.f;
+  }
+  griddep_wait();
   __syncthreads();
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
@@ -175,9 +222,10 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
     tma_load_2d(&slm[0][0], &maps.lm, Z0 - 4, X0 - 2, bar);
     tma_load_2d(&smu[0][0], &maps.mu, Z0 - 4, X0 - 2, bar);
   }
+  griddep_launch_dependents();
 
   // While the copies fly: receivers (pre-step velocities, by the first tile
-  // of each simulation) and this thread's buoyancy values for phase C.
+  // of each simulation).
   if (!ADJ && first && d.nr) {
     const float *in_vx = d.set[parity].vx, *in_vz = d.set[parity].vz;
     for (int r = threadIdx.x; r < d.nr; r += S::NT) {
@@ -186,21 +234,6 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
       d.rec_vz[(size_t)r * d.nt + it] = in_vz[c];
     }
   }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = w % S::H, q = w / S::H;
-  constexpr int KC = TX / G;  // own rows per thread
-  const int lzc = h * 32 + lane;  // own column of this thread (valid if < TZ)
-  const int gzc = Z0 + lzc;
-  const bool col_ok = lzc < TZ && gzc < nz;
-  float bb[KC];
-#pragma unroll
-  for (int k = 0; k < KC; ++k) {
-    const int gx = X0 + q + G * k;
-    bb[k] = (col_ok && gx < nx) ? __ldg(d.b + gx * ps + gzc) : 0.f;
-  }
-  // Snapshot step: forward stores the pre-step state, adjoint correlates
-  // with it (both at this shot's snapshot it / si).
-  const bool snap_io = (it % d.si) == 0 && d.accu[0] != nullptr && (ADJ || store);
-  const size_t soff = (size_t)(it / d.si) * nx * nz;
 
   // Bounded wait (about a second at most); the CTA agrees on the outcome so
   // that it leaves together, after its copies have landed.
@@ -215,9 +248,94 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
 
   const float dtv = ADJ ? -d.dt : d.dt;
   const float idx = d.idx, idz = d.idz;
-  const int np = d.np;
   const float(*VX)[W] = sv[0];
   const float(*VZ)[W] = sv1;
+
+  if (inner) {
+    // Phase B, interior: each thread walks SR / G consecutive rows of one
+    // column, keeping the x-direction stencil values of vx and vz in
+    // registers (one new shared load each per row).
+    constexpr int RB = SR / G;
+    const int c = 2 + h * 32 + lane;
+    const int gz = Z0 - 4 + c;
+    const bool z_own = c >= 4 && c < TZ + 4;
+    const int r0 = q * RB;
+    float xm1 = VX[r0 + 1][c], x0 = VX[r0 + 2][c], xp1 = VX[r0 + 3][c], xp2 = VX[r0 + 4][c];
+    float zm2 = VZ[r0][c], zm1 = VZ[r0 + 1][c], z0 = VZ[r0 + 2][c], zp1 = VZ[r0 + 3][c];
+    int gp = (X0 - 2 + r0) * ps + gz;
+#pragma unroll
+    for (int k = 0; k < RB; ++k) {
+      const int r = r0 + k, vr = r + 2;
+      const float lm = slm[r][c], mu = smu[r][c];
+      const float la = lm - 2.0f * mu;
+      const float dvx = c1 * (xp1 - x0) + c2 * (xm1 - xp2);
+      const float dvz = c1 * (z0 - VZ[vr][c - 1]) + c2 * (VZ[vr][c - 2] - VZ[vr][c + 1]);
+      const float gxz = (c1 * (VX[vr][c + 1] - x0) + c2 * (VX[vr][c - 1] - VX[vr][c + 2])) * idz +
+                        (c1 * (z0 - zm1) + c2 * (zm2 - zp1)) * idx;
+      const float ex = dvx * idx, ez = dvz * idz;
+      const float sxx = sxx_[r][c] + dtv * (lm * ex + la * ez);
+      const float szz = szz_[r][c] + dtv * (la * ex + lm * ez);
+      const float sxz = sxz_[r][c] + dtv * mu * gxz;
+      sxx_[r][c] = sxx;
+      szz_[r][c] = szz;
+      sxz_[r][c] = sxz;
+      if (z_own && r >= 2 && r < TX + 2) {
+        out.txx[gp] = sxx;
+        out.tzz[gp] = szz;
+        out.txz[gp] = sxz;
+      }
+      gp += ps;
+      if (k + 1 < RB) {
+        xm1 = x0;
+        x0 = xp1;
+        xp1 = xp2;
+        xp2 = VX[vr + 3][c];
+        zm2 = zm1;
+        zm1 = z0;
+        z0 = zp1;
+        zp1 = VZ[vr + 2][c];
+      }
+    }
+    __syncthreads();
+    // Phase C, interior: KC consecutive rows per thread with the x-direction
+    // windows of txx and txz in registers.
+    if (lzc < TZ) {
+      const float(*TXX)[W] = sxx_;
+      const float(*TZZ)[W] = szz_;
+      const float(*TXZ)[W] = sxz_;
+      const int cc = lzc + 4;
+      const int lx0 = q * KC;
+      const int s0 = lx0 + 2;  // stress box row of the first point
+      float am2 = TXX[s0 - 2][cc], am1 = TXX[s0 - 1][cc], a0 = TXX[s0][cc], ap1 = TXX[s0 + 1][cc];
+      float bm1 = TXZ[s0 - 1][cc], b0 = TXZ[s0][cc], bp1 = TXZ[s0 + 1][cc], bp2 = TXZ[s0 + 2][cc];
+      int gq = (X0 + lx0) * ps + gzc;
+#pragma unroll
+      for (int k = 0; k < KC; ++k) {
+        const int r = s0 + k, lx = lx0 + k;
+        const float ax = (c1 * (a0 - am1) + c2 * (am2 - ap1)) * idx +
+                         (c1 * (b0 - TXZ[r][cc - 1]) + c2 * (TXZ[r][cc - 2] - TXZ[r][cc + 1])) * idz;
+        const float az = (c1 * (bp1 - b0) + c2 * (bm1 - bp2)) * idx +
+                         (c1 * (TZZ[r][cc + 1] - TZZ[r][cc]) + c2 * (TZZ[r][cc - 1] - TZZ[r][cc + 2])) * idz;
+        const float bdt = bb[k] * dtv;
+        out.vx[gq] = VX[lx + 4][cc] + bdt * ax;
+        out.vz[gq] = VZ[lx + 4][cc] + bdt * az;
+        gq += ps;
+        if (k + 1 < KC) {
+          am2 = am1;
+          am1 = a0;
+          a0 = ap1;
+          ap1 = TXX[r + 2][cc];
+          bm1 = b0;
+          b0 = bp1;
+          bp1 = bp2;
+          bp2 = TXZ[r + 3][cc];
+        }
+      }
+    }
+    return;
+  }
+
+  const int np = d.np;
   // Phase B: new stresses over rows X0-2 .. X0+TX+2 and box columns
   // 2 .. TZ+6 (z = Z0-2 .. Z0+TZ+2), in place.
   {
@@ -372,9 +490,20 @@ cudaError_t launch_single(const SimDesc &d, int it, int parity, int store, int *
   cudaError_t e = configure(fused_step_tma<S, CFG, ADJ>, S::SMEM, configured);
   if (e != cudaSuccess) return e;
   const int tiles_x = (d.nx + S::TX - 1) / S::TX, tiles_z = (d.nz + S::TZ - 1) / S::TZ;
-  fused_step_tma<S, CFG, ADJ><<<tiles_x * tiles_z, S::NT, S::SMEM, s>>>(d, tiles_z, it, parity,
-                                                                        store, err);
-  return cudaGetLastError();
+  // Programmatic stream serialisation: the CTAs of this step may become
+  // resident while the previous step drains; they wait in griddep_wait
+  // before touching any wave field.
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(tiles_x * tiles_z);
+  lc.blockDim = dim3(S::NT);
+  lc.dynamicSmemBytes = S::SMEM;
+  lc.stream = s;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, fused_step_tma<S, CFG, ADJ>, d, tiles_z, it, parity, store, err);
 }
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
