@@ -196,6 +196,56 @@ def fwi_gradients(steps, warmup, with_cpu):
     return out
 
 
+def fwi_gradients_c3(steps):
+    """FWI gradients/s on the differentiation workload (1000 x 400 inner
+    cells, 8 shots, nt = 6000, FP32 wave fields, FP64 kernel sums): the
+    gradient of the L2 misfit through the torch.autograd layer, as the exact
+    discrete adjoint with checkpoints every 100 steps and with every state
+    kept, and the reference's own adjoint kernels (snapshots every 10 steps).
+    Each timed gradient starts from CUDA tensors and ends with the gradient
+    in CUDA tensors."""
+    import torch
+
+    import psvwave_gb300 as psv
+    from psvwave_gb300 import workloads
+    from psvwave_gb300.torch_ops import l2_misfit
+
+    p = workloads.c3_params()
+    true, start = workloads.c3_media(p)
+    m = psv.fdModel.from_parameters(p)
+    m.set_parameter_fields(*true)
+    for s_ in range(m.n_shots):
+        m.forward_simulate(s_, False)
+    m.set_observed_data(*m.get_synthetic_data())
+    out = {"unit": "FWI gradients/s",
+           "workload": "c3: 1100x500 grid (1000x400 inner + 50), 8 shots, nt=6000, 200 receivers, "
+                       "Ricker 25 Hz; layered + 3 elliptic vs anomalies, start = 20-cell smoothing"}
+    runs = (("checkpoint_100", dict(checkpoint_every=100, mode="exact")),
+            ("store_all", dict(checkpoint_every=p["nt"], mode="exact")),
+            ("reference_kernels", dict(checkpoint_every=100, mode="reference")))
+    for name, kw in runs:
+        def one():
+            t = [torch.tensor(a, dtype=torch.float64, device="cuda", requires_grad=True)
+                 for a in start]
+            chi = l2_misfit(m, *t, **kw)
+            chi.backward()
+            torch.cuda.synchronize()
+            return float(chi.detach())
+
+        one()  # warm-up: allocations, eager first run
+        one()  # warm-up: per-shot pipelines captured as CUDA graphs
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            chi = one()
+        dt = (time.perf_counter() - t0) / steps
+        res = {"value": 1.0 / dt, "ms_per_gradient": 1e3 * dt, "misfit": chi}
+        if kw["mode"] == "exact":
+            res["device_bytes"] = m.exact_bytes(kw["checkpoint_every"])
+        out[name] = res
+    out["value"] = out["checkpoint_100"]["value"]
+    return out
+
+
 def batched(steps, warmup):
     """Aggregate Gcell-updates/s of the batching workload (256 models of
     uneven sizes, 1-4 shots each, nt = 1000): all shots of all models in one
@@ -403,7 +453,8 @@ def main():
     if rank == 0 and not args.no_secondary:
         secondary = {"fwi_gradients": fwi_gradients(args.steps, args.warmup,
                                                     world == 1 and not args.no_cpu_baseline),
-                     "batched": batched(args.steps, args.warmup)}
+                     "batched": batched(args.steps, args.warmup),
+                     "fwi_gradients_c3": fwi_gradients_c3(min(args.steps, 2))}
 
     if rank == 0:
         line = {

@@ -1,6 +1,8 @@
 // FP64 reductions and point-wise maps on receiver data and kernels.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "psv_solver.hpp"
 
 namespace psv {
@@ -103,6 +105,39 @@ cudaError_t exact_receiver_terms(int rows, int nt, double dt, double dxdz, const
                                  const double *obs, double *adj, cudaStream_t s) {
   if (rows <= 0) return cudaSuccess;
   reverse_residual_sum<<<(rows + 127) / 128, 128, 0, s>>>(rows, nt, dt, dxdz, syn, obs, adj);
+  return cudaGetLastError();
+}
+
+struct StatePtrs {
+  const uint4 *src[5];
+  uint4 *dst[5];
+  uint4 *dst2[5];
+};
+
+__global__ void copy_state_kernel(StatePtrs p, size_t n16) {
+  const int f = blockIdx.y;
+  const uint4 *src = p.src[f];
+  uint4 *dst = p.dst[f], *dst2 = p.dst2[f];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const uint4 v = src[i];
+    dst[i] = v;
+    if (dst2) dst2[i] = v;
+  }
+}
+
+cudaError_t copy_state(const void *const src[5], void *const dst[5], void *const *dst2,
+                       size_t bytes, cudaStream_t s) {
+  StatePtrs p;
+  for (int f = 0; f < 5; ++f) {
+    p.src[f] = static_cast<const uint4 *>(src[f]);
+    p.dst[f] = static_cast<uint4 *>(dst[f]);
+    p.dst2[f] = dst2 ? static_cast<uint4 *>(dst2[f]) : nullptr;
+  }
+  const size_t n16 = bytes / 16;
+  if (n16 == 0) return cudaSuccess;
+  const unsigned bx = static_cast<unsigned>(std::min<size_t>((n16 + 255) / 256, 1216));
+  copy_state_kernel<<<dim3(bx, 5), 256, 0, s>>>(p, n16);
   return cudaGetLastError();
 }
 

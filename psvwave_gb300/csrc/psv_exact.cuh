@@ -202,19 +202,24 @@ __global__ void stress_transpose(AdjArgs<T> a) {
   }
 }
 
-// Receiver term: v-bar^n(rec) += adj[r][n] (both components), serially so
-// coinciding receivers add in a fixed order.
+// Receiver term: v-bar^n(rec) += adj[r][n] (both components). One thread
+// per (cell, component) adds the terms of the receivers at that cell in
+// increasing receiver index, so coinciding receivers add in a fixed order
+// (the same sums as one serial pass over the receivers).
 template <typename T>
-__global__ void add_receiver_terms(int nr, int nt, int it, int pitch, int nz, const int *cells,
-                                   const double *adj_x, const double *adj_z, T *lvx, T *lvz) {
-  const int comp = threadIdx.x;
-  if (comp > 1) return;
+__global__ void add_receiver_terms(int n_groups, int nt, int it, const int *cells,
+                                   const int *start, const int *order, const double *adj_x,
+                                   const double *adj_z, T *lvx, T *lvz) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 2 * n_groups) return;
+  const int grp = k >> 1, comp = k & 1;
   T *lv = comp == 0 ? lvx : lvz;
   const double *adj = comp == 0 ? adj_x : adj_z;
-  for (int r = 0; r < nr; ++r) {
-    const int c = cells[r];  // padded cell
-    lv[c] = lv[c] + (T)adj[(size_t)r * nt + it];
-  }
+  const int j0 = start[grp], j1 = start[grp + 1];
+  const int c = cells[order[j0]];  // padded cell
+  T v = lv[c];
+  for (int j = j0; j < j1; ++j) v = v + (T)adj[(size_t)order[j] * nt + it];
+  lv[c] = v;
 }
 
 }  // namespace exact
@@ -256,10 +261,10 @@ __global__ void add_receiver_terms(int nr, int nt, int it, int pitch, int nz, co
     const dim3 block(32, 8), grid((e.nz + 31) / 32, (e.nx + 7) / 8);                          \
     exact::velocity_transpose<T><<<grid, block, 0, s>>>(a, e.plan, e.stf, e.nt, e.it, e.dt);  \
     exact::stress_transpose<T><<<grid, block, 0, s>>>(a);                                     \
-    if (e.nr)                                                                                 \
-      exact::add_receiver_terms<T><<<1, 32, 0, s>>>(e.nr, e.nt, e.it, e.pitch, e.nz,         \
-                                                     e.rec_cell, e.adj_x, e.adj_z, a.lvx,     \
-                                                     a.lvz);                                  \
+    if (e.n_rec_groups)                                                                       \
+      exact::add_receiver_terms<T><<<(2 * e.n_rec_groups + 127) / 128, 128, 0, s>>>(         \
+          e.n_rec_groups, e.nt, e.it, e.rec_cell, e.rec_start, e.rec_order, e.adj_x, e.adj_z, \
+          a.lvx, a.lvz);                                                                      \
     return cudaGetLastError();                                                                \
   }                                                                                           \
   }

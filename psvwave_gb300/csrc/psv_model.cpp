@@ -242,6 +242,32 @@ void Model::allocate() {
     cuda_check(cudaMemcpy(rec_cell_.get(), cells.data(), cells.size() * sizeof(int),
                           cudaMemcpyHostToDevice),
                "upload receivers");
+  {
+    // Receivers grouped by cell, groups in order of first appearance and
+    // receivers in increasing index within a group.
+    std::vector<int> start, order;
+    std::vector<char> done(cfg_.nr, 0);
+    for (int r = 0; r < cfg_.nr; ++r) {
+      if (done[r]) continue;
+      start.push_back(static_cast<int>(order.size()));
+      for (int q = r; q < cfg_.nr; ++q)
+        if (!done[q] && cells[q] == cells[r]) {
+          order.push_back(q);
+          done[q] = 1;
+        }
+    }
+    n_rec_groups_ = static_cast<int>(start.size());
+    start.push_back(static_cast<int>(order.size()));
+    rec_start_.allocate(start.size() * sizeof(int));
+    rec_order_.allocate(std::max<size_t>(order.size(), 1) * sizeof(int));
+    cuda_check(cudaMemcpy(rec_start_.get(), start.data(), start.size() * sizeof(int),
+                          cudaMemcpyHostToDevice),
+               "upload receiver groups");
+    if (!order.empty())
+      cuda_check(cudaMemcpy(rec_order_.get(), order.data(), order.size() * sizeof(int),
+                            cudaMemcpyHostToDevice),
+                 "upload receiver groups");
+  }
   taper_tab_d_.allocate(taper_tab_.size() * e);
   if (prec_ == PSV_FP64) {
     cuda_check(cudaMemcpy(taper_tab_d_.get(), taper_tab_.data(),
@@ -458,32 +484,37 @@ double Model::exact_gradient(int C) {
   if (C <= 0 || C > nt) C = nt;
   const int n_ck = (nt + C - 1) / C;
   const size_t gp = padded_size(), g = grid_size(), e = elem();
-  const size_t state_elems = 5 * gp;
+  const size_t field_bytes = gp * e, state_bytes = 5 * field_bytes;
   cudaStream_t s = stream();
+  // Scratch grows only; captured pipelines hold its addresses, so a
+  // reallocation drops them.
+  bool grown = false;
   auto ensure = [&](DeviceBuffer &b, size_t bytes) {
-    if (b.bytes() < bytes) b.allocate(bytes);
+    if (b.bytes() < bytes) {
+      synchronize();
+      b.allocate(bytes);
+      grown = true;
+    }
   };
   for (auto &b : gex_) ensure(b, g * sizeof(double));
   for (auto &b : kexact_) ensure(b, g * sizeof(double));
   for (auto &b : adj_) ensure(b, data_size() * sizeof(double));
   for (auto &b : lam_) ensure(b, gp * e);
-  ensure(ckpt_, n_ck * state_elems * e);
-  ensure(slots_, (C + 1) * state_elems * e);
+  ensure(ckpt_, n_ck * state_bytes);
+  ensure(slots_, (C + 1) * state_bytes);
+  if (grown) clear_graphs();
   for (auto &b : gex_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "exact zero");
 
-  SolverArgs a = solver_args();
+  const SolverArgs a = solver_args();
   unsigned char *ck = ckpt_.as<unsigned char>(), *sl = slots_.as<unsigned char>();
-  auto save_state = [&](unsigned char *dst) {
-    for (int f = 0; f < 5; ++f)
-      cuda_check(cudaMemcpyAsync(dst + f * gp * e, fields_[f].get(), gp * e,
-                                 cudaMemcpyDeviceToDevice, s),
-                 "save state");
+  void *fields[5];
+  for (int f = 0; f < 5; ++f) fields[f] = fields_[f].get();
+  auto state = [&](unsigned char *base, void *out[5]) {
+    for (int f = 0; f < 5; ++f) out[f] = base + f * field_bytes;
   };
-  auto load_state = [&](const unsigned char *src) {
-    for (int f = 0; f < 5; ++f)
-      cuda_check(cudaMemcpyAsync(fields_[f].get(), src + f * gp * e, gp * e,
-                                 cudaMemcpyDeviceToDevice, s),
-                 "load state");
+  // dst <- src (and dst2 <- src), whole states.
+  auto copy = [&](void *const src[5], void *const dst[5], void *const *dst2) {
+    cuda_check(copy_state(src, dst, dst2, field_bytes, s), "copy state");
   };
   auto fwd = [&](int shot, int it0, int it1, bool finish) {
     cudaError_t err = prec_ == PSV_FP64
@@ -491,36 +522,112 @@ double Model::exact_gradient(int C) {
                           : forward_f32(a, plans_[shot], shot, false, it0, it1, false, finish, s);
     cuda_check(err, "exact forward");
   };
-  cur_ = 0;
-  // 1. Forward runs of every shot for the seismograms (and misfit).
-  for (int shot = 0; shot < n_shots; ++shot) {
-    for (auto &f : fields_) cuda_check(cudaMemsetAsync(f.get(), 0, f.bytes(), s), "zero");
-    fwd(shot, 0, nt, true);
-  }
-  const double misfit = calculate_l2_misfit();
-  // 2. Receiver terms of the adjoint.
-  for (int c = 0; c < 2; ++c)
-    cuda_check(exact_receiver_terms(n_shots * nr, nt, cfg_.dt, cfg_.dx * cfg_.dz,
-                                    rtf_[c].as<double>(), rtf_true_[c].as<double>(),
-                                    adj_[c].as<double>(), s),
-               "receiver terms");
-  // 3. Per shot: checkpointed forward, then segments backwards.
-  for (int shot = 0; shot < n_shots; ++shot) {
-    for (auto &f : fields_) cuda_check(cudaMemsetAsync(f.get(), 0, f.bytes(), s), "zero");
-    for (int k = 0; k < n_ck; ++k) {
-      save_state(ck + k * state_elems * e);
-      if (k + 1 < n_ck) fwd(shot, k * C, (k + 1) * C, false);
+  // FP32 with the TMA step: the forward runs ping-pong in the model's two
+  // field sets (checkpoint pass) and from state slot j straight into slot
+  // j + 1 (recompute), so no state is copied per step. The slots' input
+  // tensor maps are encoded once per call, when first needed.
+  const bool tma = prec_ == PSV_FP32 && tma_ok_ && variant_ == kFusedTma;
+  std::vector<tma::Maps> slot_maps;
+  auto slot_fields = [&](int j) {
+    void *p[5];
+    state(sl + j * state_bytes, p);
+    return fast::Fields{static_cast<float *>(p[0]), static_cast<float *>(p[1]),
+                        static_cast<float *>(p[2]), static_cast<float *>(p[3]),
+                        static_cast<float *>(p[4])};
+  };
+  // Steps it0 .. it1-1 of `shot` from slot 0 (state it0) into slots 1 ..
+  // it1-it0; receivers are recorded when `record`.
+  auto tma_slots = [&](int shot, int it0, int it1, bool record) {
+    if (slot_maps.empty()) {
+      slot_maps.resize(C + 1);
+      for (int j = 0; j <= C; ++j)
+        if (!tma::encode_input_maps(slot_maps[j], slot_fields(j), lm_.as<float>(), mu_.as<float>(),
+                                    geo_.nx, geo_.nz, pitch_, tile_cfg_))
+          throw Error(PSV_ERR_CUDA, "tensor-map encoding failed for a state slot");
     }
+    for (int n = it0; n < it1; ++n) {
+      const int j = n - it0;
+      tma::SimDesc d = descs_h_[shot];
+      d.set[0] = slot_fields(j);
+      d.set[1] = slot_fields(j + 1);
+      d.maps[0] = slot_maps[j];
+      if (!record) d.nr = 0;
+      cuda_check(tma::step_single(d, tile_cfg_, false, n, 0, false, err_flag_.as<int>(), s),
+                 "exact forward");
+    }
+  };
+  // One shot: checkpointed forward (which also gives the shot's seismograms
+  // and, from them, its adjoint receiver terms), then the segments
+  // backwards: each is recomputed from its checkpoint into C + 1 state slots
+  // and transposed step by step. Deterministic in (shot, C) and the scratch
+  // addresses, so it is captured once as a CUDA graph and replayed.
+  auto one_shot = [&](int shot) {
+    if (tma) {
+      // Checkpoint pass; its last segment writes its states into the slots
+      // directly, and the reverse pass starts from them.
+      const int last0 = (n_ck - 1) * C;
+      if (last0 > 0) cuda_check(tma_forward(shot, false, 0, 0, true, false, nullptr), "zero");
+      for (int k = 0; k + 1 < n_ck; ++k) {
+        void *src[5], *dst[5];
+        for (int f = 0; f < 5; ++f) src[f] = (cur_ ? fields2_ : fields_)[f].get();
+        state(ck + k * state_bytes, dst);
+        copy(src, dst, nullptr);
+        cuda_check(tma_forward(shot, false, k * C, (k + 1) * C, false, false, nullptr),
+                   "exact forward");
+      }
+      if (last0 > 0) {
+        void *src[5], *dst[5];
+        for (int f = 0; f < 5; ++f) src[f] = (cur_ ? fields2_ : fields_)[f].get();
+        state(sl, dst);
+        copy(src, dst, nullptr);
+      } else {
+        cuda_check(cudaMemsetAsync(sl, 0, state_bytes, s), "zero state");
+      }
+      tma_slots(shot, last0, nt, true);
+      if (nr) {
+        const size_t off = static_cast<size_t>(shot) * nr * nt;
+        const float *raw = rec_raw_.as<float>();
+        cuda_check(receiver_cumsum_f32(nr, nt, nt, cfg_.dt, cfg_.dx * cfg_.dz, raw,
+                                       raw + static_cast<size_t>(nr) * nt,
+                                       rtf_[0].as<double>() + off, rtf_[1].as<double>() + off, s),
+                   "seismograms");
+      }
+    } else {
+      for (auto &f : fields_) cuda_check(cudaMemsetAsync(f.get(), 0, f.bytes(), s), "zero");
+      for (int k = 0; k < n_ck; ++k) {
+        void *dst[5];
+        state(ck + k * state_bytes, dst);
+        copy(fields, dst, nullptr);
+        fwd(shot, k * C, std::min(nt, (k + 1) * C), k + 1 == n_ck);
+      }
+    }
+    const size_t off = static_cast<size_t>(shot) * nr * nt;
+    for (int c = 0; c < 2; ++c)
+      cuda_check(exact_receiver_terms(nr, nt, cfg_.dt, cfg_.dx * cfg_.dz, rtf_[c].as<double>() + off,
+                                      rtf_true_[c].as<double>() + off, adj_[c].as<double>() + off,
+                                      s),
+                 "receiver terms");
     for (auto &b : lam_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "zero adjoint");
     void *lt[3] = {lam_[2].get(), lam_[3].get(), lam_[4].get()};
     void *ot[3] = {lam_[5].get(), lam_[6].get(), lam_[7].get()};
     for (int k = n_ck - 1; k >= 0; --k) {
       const int s0 = k * C, s1 = std::min(nt, s0 + C);
-      load_state(ck + k * state_elems * e);
-      save_state(sl);
-      for (int n = s0; n < s1; ++n) {
-        fwd(shot, n, n + 1, false);
-        save_state(sl + (n + 1 - s0) * state_elems * e);
+      void *src[5], *slot0[5];
+      state(ck + k * state_bytes, src);
+      state(sl, slot0);
+      if (tma) {
+        if (k + 1 < n_ck) {  // the last segment's states are already in the slots
+          copy(src, slot0, nullptr);
+          tma_slots(shot, s0, s1, false);
+        }
+      } else {
+        copy(src, fields, slot0);
+        for (int n = s0; n < s1; ++n) {
+          void *dst[5];
+          state(sl + (n + 1 - s0) * state_bytes, dst);
+          fwd(shot, n, n + 1, false);
+          copy(fields, dst, nullptr);
+        }
       }
       for (int n = s1 - 1; n >= s0; --n) {
         ExactStepArgs x;
@@ -545,13 +652,13 @@ double Model::exact_gradient(int C) {
           x.lt[f] = lt[f];
           x.ot[f] = ot[f];
         }
-        const unsigned char *sv = sl + (n - s0) * state_elems * e;      // v^n
-        const unsigned char *st = sl + (n + 1 - s0) * state_elems * e;  // tau^(n+1)
+        const unsigned char *sv = sl + (n - s0) * state_bytes;      // v^n
+        const unsigned char *st = sl + (n + 1 - s0) * state_bytes;  // tau^(n+1)
         x.fv[0] = sv;
-        x.fv[1] = sv + gp * e;
-        x.ft[0] = st + 2 * gp * e;
-        x.ft[1] = st + 3 * gp * e;
-        x.ft[2] = st + 4 * gp * e;
+        x.fv[1] = sv + field_bytes;
+        x.ft[0] = st + 2 * field_bytes;
+        x.ft[1] = st + 3 * field_bytes;
+        x.ft[2] = st + 4 * field_bytes;
         x.g_lm = gex_[0].as<double>();
         x.g_la = gex_[1].as<double>();
         x.g_mu = gex_[2].as<double>();
@@ -559,22 +666,29 @@ double Model::exact_gradient(int C) {
         x.plan = plans_[shot];
         x.stf = stf_d_.as<double>();
         x.rec_cell = rec_cell_.as<int>();
-        x.adj_x = adj_[0].as<double>() + static_cast<size_t>(shot) * nr * nt;
-        x.adj_z = adj_[1].as<double>() + static_cast<size_t>(shot) * nr * nt;
+        x.n_rec_groups = n_rec_groups_;
+        x.rec_start = rec_start_.as<int>();
+        x.rec_order = rec_order_.as<int>();
+        x.adj_x = adj_[0].as<double>() + off;
+        x.adj_z = adj_[1].as<double>() + off;
         cuda_check(prec_ == PSV_FP64 ? exact_step_f64(x, s) : exact_step_f32(x, s), "exact step");
         std::swap(lt[0], ot[0]);
         std::swap(lt[1], ot[1]);
         std::swap(lt[2], ot[2]);
       }
     }
-  }
-  // 4. Chain rule to (vp, vs, rho).
+  };
+  cur_ = 0;
+  for (int shot = 0; shot < n_shots; ++shot) run_loop(2, shot, false, C, [&] { one_shot(shot); });
+  const double misfit = calculate_l2_misfit();
+  // Chain rule to (vp, vs, rho).
   cuda_check(exact_chain(g, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(),
                          gex_[0].as<double>(), gex_[1].as<double>(), gex_[2].as<double>(),
                          gex_[3].as<double>(), kexact_[0].as<double>(), kexact_[1].as<double>(),
                          kexact_[2].as<double>(), s),
              "exact chain");
   synchronize();
+  if (tma) check_device_error();
   return misfit;
 }
 

@@ -222,6 +222,8 @@ class Model {
   DeviceBuffer rtf_[2], rtf_true_[2], a_stf_[2];  // data          (FP64)
   DeviceBuffer rec_raw_;                      // [2][nr][nt]         (T)
   DeviceBuffer rec_cell_;                     // [nr] int
+  DeviceBuffer rec_start_, rec_order_;        // receivers grouped by cell (exact adjoint)
+  int n_rec_groups_ = 0;
   DeviceBuffer stf_d_;                        // [n_sources][nt]     (FP64)
   DeviceBuffer klame_[3];                     // lambda mu rho       (FP64)
   DeviceBuffer kvel_[3];                      // vp vs rho           (FP64)

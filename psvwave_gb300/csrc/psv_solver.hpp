@@ -111,6 +111,10 @@ struct ExactStepArgs {
   InjPlan plan{};
   const double *stf = nullptr;
   const int *rec_cell = nullptr;           // padded receiver cells
+  // Receivers grouped by cell: group g holds receivers
+  // rec_order[rec_start[g] .. rec_start[g+1]) in increasing index.
+  int n_rec_groups = 0;
+  const int *rec_start = nullptr, *rec_order = nullptr;
   const double *adj_x = nullptr, *adj_z = nullptr;  // receiver terms [nr][nt] of the shot
 };
 cudaError_t exact_step_f32(const ExactStepArgs &e, cudaStream_t s);
@@ -135,6 +139,11 @@ cudaError_t map_kernels(size_t n, const double *vp, const double *vs, const doub
 // sum_{m >= n} dt (syn[r][m] - obs[r][m]), per receiver row of length nt.
 cudaError_t exact_receiver_terms(int rows, int nt, double dt, double dxdz, const double *syn,
                                  const double *obs, double *adj, cudaStream_t s);
+// Copies five wave-field arrays of `bytes` each (a multiple of 16, all
+// pointers 16-byte aligned) from src[f] to dst[f], and to dst2[f] too when
+// dst2 is non-null: one launch for a whole state.
+cudaError_t copy_state(const void *const src[5], void *const dst[5], void *const *dst2,
+                       size_t bytes, cudaStream_t s);
 // Gradients with respect to (vp, vs, rho) from those with respect to
 // (lm, la, mu, b): lm = rho vp^2, la = rho (vp^2 - 2 vs^2), mu = rho vs^2,
 // b = 1 / rho.

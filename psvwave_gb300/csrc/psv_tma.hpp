@@ -53,6 +53,10 @@ bool supported(int nx, int nz, int pitch);
 // Encodes desc.maps for tile shape `cfg` from desc.set, desc.lm and the mu
 // array; false on failure.
 bool make_maps(SimDesc &desc, const float *mu, int cfg);
+// Encodes the tensor maps that read the wave-field set `in` (with the medium
+// lm, mu) for tile shape `cfg`; false on failure.
+bool encode_input_maps(Maps &m, const fast::Fields &in, const float *lm, const float *mu, int nx,
+                       int nz, int pitch, int cfg);
 
 // Appends the tiles of simulation `sim` (one int4 per CTA: sim, x0, z0,
 // first-tile flag) for tile shape `cfg`.

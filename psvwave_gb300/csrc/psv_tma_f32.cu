@@ -570,6 +570,12 @@ bool make_maps(SimDesc &d, const float *mu, int cfg) {
   return true;
 }
 
+bool encode_input_maps(Maps &m, const fast::Fields &in, const float *lm, const float *mu, int nx,
+                       int nz, int pitch, int cfg) {
+  return cfg == kTile16x28 ? encode_set<Small>(m, in, lm, mu, nx, nz, pitch)
+                           : encode_set<Big>(m, in, lm, mu, nx, nz, pitch);
+}
+
 void append_tiles(int cfg, int sim, int nx, int nz, std::vector<int4> &tiles) {
   int tx, tz;
   tile_dims(cfg, &tx, &tz);

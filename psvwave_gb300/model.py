@@ -234,13 +234,17 @@ class fdModel:
         self.run_model(verbose=verbose, simulate_adjoint=True)
         return self.misfit, self.get_gradient_vector()
 
-    def exact_gradient(self, checkpoint_every=100):
+    def exact_gradient(self, checkpoint_every=100, on_device=False):
         """Misfit and its gradient with respect to (vp, vs, rho) over all
         shots by the exact discrete adjoint (the transpose of the time
         stepping), with forward states rebuilt from checkpoints every
-        `checkpoint_every` steps. Returns (misfit, (g_vp, g_vs, g_rho))."""
+        `checkpoint_every` steps. Returns (misfit, (g_vp, g_vs, g_rho)),
+        numpy arrays, or CUDA tensors with on_device=True."""
         mis = ctypes.c_double()
         _capi.check(self._lib.psv_exact_gradient(self._h, int(checkpoint_every), ctypes.byref(mis)))
+        if on_device:
+            self._info.misfit = mis.value
+            return mis.value, self.get_exact_gradient_device()
         g = [_out((self.nx, self.nz)) for _ in range(3)]
         _capi.check(self._lib.psv_get_exact_gradient(self._h, *[_ptr(a) for a in g]))
         self._info.misfit = mis.value
@@ -419,6 +423,56 @@ class fdModel:
         n = ctypes.c_size_t()
         _capi.check(self._lib.psv_device_bytes(self._h, ctypes.byref(n)))
         return n.value
+
+    # Device buffers (torch CUDA tensors, float64, contiguous). Inputs are read
+    # on this model's stream after the caller's current stream has finished
+    # with them; outputs are complete when the call returns.
+    def _device_tensor(self, t, shape, name):
+        import torch
+
+        if tuple(t.shape) != tuple(shape):
+            raise ValueError("The input tensor %s does not have the right shape." % name)
+        if not t.is_cuda or t.device.index != self.device:
+            raise ValueError("tensor %s must live on cuda:%d" % (name, self.device))
+        t = t.detach().to(torch.float64).contiguous()
+        torch.cuda.current_stream(t.device).synchronize()
+        return t
+
+    def _device_out(self, shape):
+        import torch
+
+        return torch.empty(shape, dtype=torch.float64, device="cuda:%d" % self.device)
+
+    def set_parameter_fields_device(self, vp, vs, rho):
+        """set_parameter_fields from CUDA tensors [nx, nz]."""
+        shape = (self.nx, self.nz)
+        t = [self._device_tensor(a, shape, n) for a, n in zip((vp, vs, rho), ("_vp", "_vs", "_rho"))]
+        _capi.check(self._lib.psv_set_parameter_fields_device(
+            self._h, *[ctypes.cast(x.data_ptr(), _DP) for x in t]))
+
+    def set_observed_data_device(self, ux, uz):
+        t = [self._device_tensor(a, self._data_shape(), n) for a, n in ((ux, "ux"), (uz, "uz"))]
+        _capi.check(self._lib.psv_set_observed_data_device(
+            self._h, *[ctypes.cast(x.data_ptr(), _DP) for x in t]))
+
+    def get_synthetic_data_device(self):
+        out = [self._device_out(self._data_shape()) for _ in range(2)]
+        _capi.check(self._lib.psv_get_synthetic_data_device(
+            self._h, *[ctypes.cast(x.data_ptr(), _DP) for x in out]))
+        return tuple(out)
+
+    def get_kernels_device(self):
+        out = [self._device_out((self.nx, self.nz)) for _ in range(3)]
+        _capi.check(self._lib.psv_get_kernels_device(
+            self._h, *[ctypes.cast(x.data_ptr(), _DP) for x in out]))
+        return tuple(out)
+
+    def get_exact_gradient_device(self):
+        """The last exact_gradient as CUDA tensors (g_vp, g_vs, g_rho)."""
+        out = [self._device_out((self.nx, self.nz)) for _ in range(3)]
+        _capi.check(self._lib.psv_get_exact_gradient_device(
+            self._h, *[ctypes.cast(x.data_ptr(), _DP) for x in out]))
+        return tuple(out)
 
     def profile_forward(self, i_shot=0, n_steps=100):
         """Average device time (ms) per forward time step and per launch of

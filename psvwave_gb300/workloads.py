@@ -13,6 +13,13 @@ media (vp, vs, rho on the padded [nx][nz] grid).
   (Gardner), times a smooth Gaussian random field (sigma 5 %, correlation
   length 40 cells); one dipping source (45 degrees), Ricker 15 Hz; 400
   receivers along z = 5.
+* c2 -- many models of uneven sizes (c2_models).
+* c3 -- 1000 x 400 inner cells, 50-cell boundary, dx = dz = 5, dt = 4e-4
+  (CFL number 0.59 at vp 4500), nt = 6000; 8 shots of one 45-degree source
+  each, evenly spaced along z = 10, Ricker 25 Hz; 200 receivers along
+  z = 5. True medium: 30 layers as c1 (no random field) plus 3 seeded
+  elliptic anomalies of +-15 % vs; start medium: the true one smoothed by a
+  Gaussian of 20 cells.
 """
 import numpy as np
 
@@ -116,3 +123,56 @@ def c2_models(n_models=256, nt=1000, seed=2):
                               corr_len=20.0)
         out.append((p, media))
     return out
+
+
+def c3_params(nt=6000, n_shots=8, nx_inner=1000, nz_inner=400, n_rec=200):
+    """The differentiation workload (smaller variants for tests: fewer steps,
+    shots, cells or receivers)."""
+    xs = [int(nx_inner * (k + 0.5) / n_shots) for k in range(n_shots)]
+    rec = [int(2 + (nx_inner - 4) * r / max(1, n_rec - 1)) for r in range(n_rec)]
+    return dict(nt=nt, nx_inner=nx_inner, nz_inner=nz_inner, nx_inner_boundary=10,
+                nz_inner_boundary=10, dx=5.0, dz=5.0, dt=4e-4, np_boundary=50, np_factor=0.015,
+                scalar_rho=2000.0, scalar_vp=2500.0, scalar_vs=1445.0, npx=1, npz=1,
+                peak_frequency=25.0, source_timeshift=0.0, delay_cycles_per_shot=0,
+                n_sources=n_shots, ix_sources=xs, iz_sources=[10] * n_shots,
+                moment_angles=[45.0] * n_shots,
+                which_source_to_fire_in_which_shot=[[k] for k in range(n_shots)], nr=n_rec,
+                ix_receivers=rec, iz_receivers=[5] * n_rec, snapshot_interval=10)
+
+
+def gaussian_smooth(a, sigma):
+    """Gaussian smoothing with edge replication (FFT on a padded copy)."""
+    pad = int(4 * sigma)
+    b = np.pad(a, pad, mode="edge")
+    kx = np.fft.fftfreq(b.shape[0])[:, None]
+    kz = np.fft.rfftfreq(b.shape[1])[None, :]
+    filt = np.exp(-2.0 * (np.pi * sigma) ** 2 * (kx ** 2 + kz ** 2))
+    out = np.fft.irfft2(np.fft.rfft2(b) * filt, s=b.shape)
+    return out[pad:pad + a.shape[0], pad:pad + a.shape[1]]
+
+
+def c3_media(params=None, seed=3):
+    """(true, start) media of the differentiation workload for `params`
+    (default c3_params())."""
+    p = params or c3_params()
+    nb = p["np_boundary"]
+    nx, nz = p["nx_inner"] + 2 * nb, p["nz_inner"] + 2 * nb
+    rng = np.random.default_rng(seed)
+    vps = np.sort(rng.uniform(1500.0, 4500.0, 30))
+    inner = nz - 2 * nb
+    depth = np.clip(np.arange(nz) - nb, 0, inner - 1)
+    vp = np.repeat(vps[np.minimum((depth * 30) // inner, 29)][None, :], nx, axis=0)
+    vs = vp / 1.73
+    x = np.arange(nx)[:, None]
+    z = np.arange(nz)[None, :]
+    for sign in (1.0, -1.0, 1.0):
+        cx = nb + rng.uniform(0.15, 0.85) * p["nx_inner"]
+        cz = nb + rng.uniform(0.3, 0.8) * p["nz_inner"]
+        ax = rng.uniform(0.04, 0.1) * p["nx_inner"]
+        az = rng.uniform(0.04, 0.1) * p["nz_inner"]
+        inside = ((x - cx) / ax) ** 2 + ((z - cz) / az) ** 2 < 1.0
+        vs = np.where(inside, vs * (1.0 + sign * 0.15), vs)
+    rho = 310.0 * vp ** 0.25
+    true = (vp, vs, rho)
+    start = tuple(gaussian_smooth(a, 20.0) for a in true)
+    return true, start

@@ -113,3 +113,15 @@ def test_reference_kernels_point_the_same_way(golden):
         cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b)))
         print("cosine(exact, reference) %s: %.4f" % (name, cos))
         assert cos > 0.9
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_exact_gradient_graph_replay_is_bitwise(golden, precision):
+    # First call eager, second captured into per-shot CUDA graphs, third
+    # replayed: all three give the same misfit and gradient bit for bit.
+    m = setup(golden, precision)
+    runs = [m.exact_gradient(40) for _ in range(3)]
+    for mis, g in runs[1:]:
+        assert mis == runs[0][0]
+        for a, b in zip(g, runs[0][1]):
+            assert np.array_equal(a, b)
