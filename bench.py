@@ -246,6 +246,22 @@ def fwi_gradients_c3(steps):
     return out
 
 
+def mc_samples_c4():
+    """Accepted MC samples/s on the surrogate workload (c0 grid, 600 coarse
+    parameters): delayed-acceptance HMC screened by the trained network
+    (2048 prior triples + 512 local triples here; python -m
+    psvwave_gb300.c4 runs the full 20000), against HMC with the solver's
+    exact gradients and against screening by the prior alone."""
+    from psvwave_gb300 import c4
+
+    out = c4.run(n_train=2048, n_local=512, n_chains=128, n_iter=40, plain_iter=3)
+    out["unit"] = "accepted samples/s"
+    out["workload"] = ("c4: 250x150 grid, nt=2000, Ricker 15 Hz, 600 coarse parameters "
+                       "(20x10 vp/vs/rho, prior sigma 10%), s2 = misfit(prior mean)/20; "
+                       "128 chains")
+    return out
+
+
 def batched(steps, warmup):
     """Aggregate Gcell-updates/s of the batching workload (256 models of
     uneven sizes, 1-4 shots each, nt = 1000): all shots of all models in one
@@ -454,7 +470,8 @@ def main():
         secondary = {"fwi_gradients": fwi_gradients(args.steps, args.warmup,
                                                     world == 1 and not args.no_cpu_baseline),
                      "batched": batched(args.steps, args.warmup),
-                     "fwi_gradients_c3": fwi_gradients_c3(min(args.steps, 2))}
+                     "fwi_gradients_c3": fwi_gradients_c3(min(args.steps, 2)),
+                     "mc_samples_c4": mc_samples_c4()}
 
     if rank == 0:
         line = {

@@ -289,6 +289,10 @@ int psv_batch_forward(psv_batch *b, int store_fields, int n_steps);
 int psv_batch_set_tile_shape(psv_batch *b, int shape);
 int psv_batch_autotune(psv_batch *b, int n_steps, int *chosen);
 int psv_batch_info(const psv_batch *b, int *members, int *tiles, double *cells);
+/* Which members (in the order added) the next psv_batch_forward advances:
+ * flags[k] != 0; NULL = all (the default). Inactive members' CTAs exit at
+ * once, so the captured time loop serves every subset. */
+int psv_batch_set_active(psv_batch *b, const int *flags, int n);
 
 /* ---- no-allocation entry point ------------------------------------------ */
 /* L2 misfit 0.5 dt sum((obs - syn)^2) over both components, written to the

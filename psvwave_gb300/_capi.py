@@ -127,7 +127,23 @@ _SIGNATURES = {
     "psv_batch_set_tile_shape": [_vp, _c_int],
     "psv_batch_autotune": [_vp, _c_int, _ip],
     "psv_batch_info": [_vp, _ip, _ip, _dp],
+    "psv_batch_set_active": [_vp, _ip, _c_int],
     "psv_l2_misfit_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_size_t, _c_double, _vp, _vp],
+    # include/psvwave_surrogate.h
+    "psv_coarse_create": [_c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _dp, _dp,
+                          ctypes.POINTER(_vp)],
+    "psv_coarse_destroy": [_vp],
+    "psv_coarse_to_fields": [_vp, _c_int, _vp, _vp, _vp],
+    "psv_coarse_gradient": [_vp, _c_int, _vp, _vp, _c_double, _vp],
+    "psv_cnn_create": [_c_int, _c_int, ctypes.POINTER(_vp)],
+    "psv_cnn_destroy": [_vp],
+    "psv_cnn_num_params": [ctypes.POINTER(ctypes.c_size_t)],
+    "psv_cnn_set_params": [_vp, _vp],
+    "psv_cnn_get_params": [_vp, _vp],
+    "psv_cnn_predict": [_vp, _c_int, _vp, _vp, _vp],
+    "psv_cnn_loss_grad": [_vp, _c_int, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, _dp, _vp],
+    "psv_cnn_train_step": [_vp, _c_int, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
+                           ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _dp],
 }
 _RESTYPES = {"psv_last_error": ctypes.c_char_p, "psv_step_kernel_name": ctypes.c_char_p}
 

@@ -38,6 +38,17 @@ class Batch:
         for s in range(model.n_shots):
             self.add(model, s)
 
+    def set_active(self, mask=None):
+        """Members the next forward() advances (a boolean per member, in the
+        order added); None = all."""
+        if mask is None:
+            _capi.check(self._lib.psv_batch_set_active(self._h, None, len(self._models)))
+            return
+        import numpy as np
+        flags = np.ascontiguousarray(np.asarray(mask, dtype=bool).astype(np.int32))
+        _capi.check(self._lib.psv_batch_set_active(
+            self._h, flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), flags.size))
+
     def forward(self, store_fields=False, n_steps=0):
         _capi.check(self._lib.psv_batch_forward(self._h, int(bool(store_fields)), int(n_steps)))
 

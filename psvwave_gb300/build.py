@@ -37,6 +37,8 @@ UNITS = [
     ("psv_model.cpp", []),
     ("psv_batch.cpp", []),
     ("psv_capi.cpp", []),
+    ("psv_cnn.cu", []),
+    ("psv_surrogate_capi.cpp", []),
 ]
 
 

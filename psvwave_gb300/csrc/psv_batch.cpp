@@ -50,6 +50,7 @@ void Batch::add(Model *m, int shot) {
     throw Error(PSV_ERR_INVALID_ARGUMENT, "all members of a batch must share nt");
   nt_ = m->config().nt;
   members_.emplace_back(m, shot);
+  active_h_.push_back(1);
   built_ = false;
   clear_graphs();
 }
@@ -114,6 +115,7 @@ void Batch::build() {
     for (int cfg = 0; cfg < tma::kNumTileCfgs; ++cfg)
       tma::append_tiles(cfg, static_cast<int>(k), g.nx, g.nz, tiles[cfg]);
   }
+  active_.allocate(members_.size() * sizeof(int));
   descs_d_.allocate(descs.size() * sizeof(tma::SimDesc));
   cuda_check(cudaMemcpy(descs_d_.get(), descs.data(), descs.size() * sizeof(tma::SimDesc),
                         cudaMemcpyHostToDevice),
@@ -134,6 +136,11 @@ void Batch::set_tile_cfg(int cfg) {
   clear_graphs();
   tile_cfg_ = cfg;
   built_ = false;  // the descriptors' tensor maps depend on the tile shape
+}
+
+void Batch::set_active(const int *flags, int n) {
+  if (n != size()) throw Error(PSV_ERR_INVALID_ARGUMENT, "one flag per batch member is needed");
+  for (int k = 0; k < n; ++k) active_h_[k] = flags ? (flags[k] != 0) : 1;
 }
 
 void Batch::synchronize() { cuda_check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize"); }
@@ -159,10 +166,13 @@ void Batch::forward(bool store, int n_steps) {
       clear_graphs();
     }
   }
-  if (!built_) {
-    for (auto &mb : members_) mb.first->synchronize();
-    build();
-  }
+  // Members' own streams may still be updating their media.
+  for (auto &mb : members_) mb.first->synchronize();
+  if (!built_) build();
+  // The flags live in device memory that the (captured) step launches read.
+  cuda_check(cudaMemcpyAsync(active_.get(), active_h_.data(), active_h_.size() * sizeof(int),
+                             cudaMemcpyHostToDevice, stream_),
+             "batch active flags");
   const int steps = (n_steps <= 0 || n_steps > nt_) ? nt_ : n_steps;
   const int cfg = tile_cfg_;
   auto enqueue = [&]() {
@@ -170,7 +180,8 @@ void Batch::forward(bool store, int n_steps) {
     int parity = 0;
     for (int it = 0; it < steps; ++it) {
       cuda_check(tma::step(descs_d_.as<tma::SimDesc>(), tiles_d_[cfg].as<int4>(), n_tiles_[cfg],
-                           cfg, false, it, parity, store, err_flag_.as<int>(), stream_),
+                           active_.as<int>(), cfg, false, it, parity, store,
+                           err_flag_.as<int>(), stream_),
                  "batch step");
       parity ^= 1;
     }

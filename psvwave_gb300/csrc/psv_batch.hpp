@@ -32,6 +32,9 @@ class Batch {
   // Times every tile shape on n_steps steps and keeps the fastest.
   int autotune(int n_steps);
   void set_tile_cfg(int cfg);
+  // Which members the next forward() advances (non-zero = advance); all of
+  // them by default. The others keep their previous seismograms.
+  void set_active(const int *flags, int n);
   int tile_cfg() const { return tile_cfg_; }
   int size() const { return static_cast<int>(members_.size()); }
   double cells() const;  // grid points summed over members
@@ -54,6 +57,8 @@ class Batch {
   DeviceBuffer tiles_d_[tma::kNumTileCfgs];
   int n_tiles_[tma::kNumTileCfgs] = {};
   DeviceBuffer err_flag_;
+  DeviceBuffer active_;              // per member flag, read by the step kernel
+  std::vector<int> active_h_;
   std::vector<size_t> raw_off_;  // per member, floats into raw_
   struct Graph {
     cudaGraphExec_t exec = nullptr;

@@ -607,6 +607,13 @@ int psv_batch_autotune(psv_batch *b, int n_steps, int *chosen) {
   });
 }
 
+int psv_batch_set_active(psv_batch *b, const int *flags, int n) {
+  return guarded([&] {
+    need(b, "batch");
+    b->impl.set_active(flags, n);
+  });
+}
+
 int psv_batch_info(const psv_batch *b, int *members, int *tiles, double *cells) {
   return guarded([&] {
     need(b, "batch");

@@ -1,0 +1,650 @@
+// Surrogate network kernels (forward, backward, Adam) and the coarse-to-grid
+// parameter map of the Monte Carlo workload; see psv_cnn.hpp.
+//
+// Convolutions run one CTA per (sample, block of 8 output channels): the
+// sample's input channels [cin][20 x 10] are staged in shared memory with the
+// block's BF16 weights, and each of 200 threads computes one output pixel of
+// the 8 channels with FP32 FMAs. The backward pass mirrors it: input
+// gradients per (sample, block of 8 input channels), with the next layer's
+// ReLU mask fused in; weight gradients per (output channel, batch chunk) as
+// fixed-order partial sums that a second kernel adds up.
+#include "psv_cnn.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "../../include/psvwave.h"
+
+namespace psv {
+namespace cnn {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kBlk = 8;  // output (forward) or input (backward) channels per CTA
+
+size_t layer_size(int l) { return (size_t)kCout[l] * kCin[l] * 9 + kCout[l]; }
+
+size_t conv_smem() { return (size_t)kMaxC * kP * sizeof(float) + (size_t)kBlk * kMaxC * 9 * 2; }
+
+__device__ __forceinline__ void tap(int k, int dil, int &dh, int &dc) {
+  dh = (k / 3 - 1) * dil;
+  dc = (k % 3 - 1) * dil;
+}
+
+// y[b][co][p] = bias[co] + sum_ci sum_k w[co][ci][k] x[b][ci][p + off_k]
+template <bool RELU>
+__global__ void __launch_bounds__(kThreads) conv_forward(int cin, int cout, int dil,
+                                                         const float *__restrict__ x,
+                                                         const __nv_bfloat16 *__restrict__ w,
+                                                         const float *__restrict__ bias,
+                                                         float *__restrict__ y) {
+  extern __shared__ float sm[];
+  float *xs = sm;                                                           // [cin][kP]
+  __nv_bfloat16 *ws = reinterpret_cast<__nv_bfloat16 *>(sm + kMaxC * kP);  // [kBlk][cin][9]
+  const int b = blockIdx.x, co0 = blockIdx.y * kBlk;
+  const int nco = min(kBlk, cout - co0);
+  const float *xb = x + (size_t)b * cin * kP;
+  for (int i = threadIdx.x; i < cin * kP; i += blockDim.x) xs[i] = xb[i];
+  for (int i = threadIdx.x; i < nco * cin * 9; i += blockDim.x) ws[i] = w[(size_t)co0 * cin * 9 + i];
+  __syncthreads();
+  const int p = threadIdx.x;
+  if (p >= kP) return;
+  const int h = p / kW, c = p - h * kW;
+  int nb[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    int dh, dc;
+    tap(k, dil, dh, dc);
+    const int hh = h + dh, cc = c + dc;
+    nb[k] = (hh >= 0 && hh < kH && cc >= 0 && cc < kW) ? hh * kW + cc : -1;
+  }
+  float acc[kBlk];
+#pragma unroll
+  for (int o = 0; o < kBlk; ++o) acc[o] = 0.f;
+  for (int ci = 0; ci < cin; ++ci) {
+    const float *xr = xs + ci * kP;
+    float v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = nb[k] >= 0 ? xr[nb[k]] : 0.f;
+#pragma unroll
+    for (int o = 0; o < kBlk; ++o) {
+      if (o < nco) {
+        const __nv_bfloat16 *wr = ws + (o * cin + ci) * 9;
+        float a = acc[o];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a = fmaf(__bfloat162float(wr[k]), v[k], a);
+        acc[o] = a;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < kBlk; ++o) {
+    if (o < nco) {
+      float r = acc[o] + bias[co0 + o];
+      if (RELU) r = fmaxf(r, 0.f);
+      y[((size_t)b * cout + co0 + o) * kP + p] = r;
+    }
+  }
+}
+
+// dx[b][ci][p] = (sum_co sum_k w[co][ci][k] dy[b][co][p - off_k]) * [act[b][ci][p] > 0]
+__global__ void __launch_bounds__(kThreads) conv_backward_data(int cin, int cout, int dil,
+                                                               const float *__restrict__ dy,
+                                                               const __nv_bfloat16 *__restrict__ w,
+                                                               const float *__restrict__ act,
+                                                               float *__restrict__ dx) {
+  extern __shared__ float sm[];
+  float *ds = sm;                                                           // [cout][kP]
+  __nv_bfloat16 *ws = reinterpret_cast<__nv_bfloat16 *>(sm + kMaxC * kP);  // [kBlk][cout][9]
+  const int b = blockIdx.x, ci0 = blockIdx.y * kBlk;
+  const int nci = min(kBlk, cin - ci0);
+  const float *db = dy + (size_t)b * cout * kP;
+  for (int i = threadIdx.x; i < cout * kP; i += blockDim.x) ds[i] = db[i];
+  for (int i = threadIdx.x; i < nci * cout * 9; i += blockDim.x) {
+    const int ci = i / (cout * 9), r = i - ci * cout * 9, co = r / 9, k = r - co * 9;
+    ws[i] = w[((size_t)co * cin + ci0 + ci) * 9 + k];
+  }
+  __syncthreads();
+  const int p = threadIdx.x;
+  if (p >= kP) return;
+  const int h = p / kW, c = p - h * kW;
+  int nb[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    int dh, dc;
+    tap(k, dil, dh, dc);
+    const int hh = h - dh, cc = c - dc;
+    nb[k] = (hh >= 0 && hh < kH && cc >= 0 && cc < kW) ? hh * kW + cc : -1;
+  }
+  float acc[kBlk];
+#pragma unroll
+  for (int o = 0; o < kBlk; ++o) acc[o] = 0.f;
+  for (int co = 0; co < cout; ++co) {
+    const float *dr = ds + co * kP;
+    float v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = nb[k] >= 0 ? dr[nb[k]] : 0.f;
+#pragma unroll
+    for (int o = 0; o < kBlk; ++o) {
+      if (o < nci) {
+        const __nv_bfloat16 *wr = ws + (o * cout + co) * 9;
+        float a = acc[o];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a = fmaf(__bfloat162float(wr[k]), v[k], a);
+        acc[o] = a;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < kBlk; ++o) {
+    if (o < nci) {
+      const size_t i = ((size_t)b * cin + ci0 + o) * kP + p;
+      dx[i] = act[i] > 0.f ? acc[o] : 0.f;
+    }
+  }
+}
+
+// Partial weight and bias gradients of output channel blockIdx.x over the
+// samples of batch chunk blockIdx.y: partial[chunk][(co*cin+ci)*9+k] and
+// partial[chunk][cout*cin*9 + co].
+__global__ void __launch_bounds__(kThreads) conv_backward_weight(int batch, int cin, int cout,
+                                                                 int dil,
+                                                                 const float *__restrict__ x,
+                                                                 const float *__restrict__ dy,
+                                                                 float *__restrict__ partial) {
+  extern __shared__ float sm[];
+  float *xs = sm;                // [cin][kP]
+  float *ds = sm + kMaxC * kP;   // [kP]
+  const int co = blockIdx.x, chunk = blockIdx.y;
+  const int b0 = (int)((long long)batch * chunk / kChunks);
+  const int b1 = (int)((long long)batch * (chunk + 1) / kChunks);
+  const int nslot = cin * 9 + 1;  // the last slot is the bias
+  constexpr int kSlots = (kMaxC * 9 + 1 + kThreads - 1) / kThreads;
+  float acc[kSlots];
+#pragma unroll
+  for (int j = 0; j < kSlots; ++j) acc[j] = 0.f;
+  for (int b = b0; b < b1; ++b) {
+    const float *xb = x + (size_t)b * cin * kP;
+    for (int i = threadIdx.x; i < cin * kP; i += blockDim.x) xs[i] = xb[i];
+    for (int i = threadIdx.x; i < kP; i += blockDim.x) ds[i] = dy[((size_t)b * cout + co) * kP + i];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kSlots; ++j) {
+      const int s = threadIdx.x + j * kThreads;
+      if (s >= nslot) continue;
+      float a = acc[j];
+      if (s == nslot - 1) {
+        for (int p = 0; p < kP; ++p) a += ds[p];
+      } else {
+        const int ci = s / 9, k = s - ci * 9;
+        int dh, dc;
+        tap(k, dil, dh, dc);
+        const float *xr = xs + ci * kP;
+        const int h0 = max(0, -dh), h1 = min(kH, kH - dh);
+        const int c0 = max(0, -dc), c1 = min(kW, kW - dc);
+        for (int h = h0; h < h1; ++h)
+          for (int c = c0; c < c1; ++c) a = fmaf(ds[h * kW + c], xr[(h + dh) * kW + c + dc], a);
+      }
+      acc[j] = a;
+    }
+    __syncthreads();
+  }
+  const size_t len = (size_t)cout * cin * 9 + cout;
+  float *out = partial + (size_t)chunk * len;
+#pragma unroll
+  for (int j = 0; j < kSlots; ++j) {
+    const int s = threadIdx.x + j * kThreads;
+    if (s >= nslot) continue;
+    if (s == nslot - 1)
+      out[(size_t)cout * cin * 9 + co] = acc[j];
+    else
+      out[(size_t)co * cin * 9 + s] = acc[j];
+  }
+}
+
+__global__ void sum_chunks(size_t len, const float *__restrict__ partial, float *__restrict__ out) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  float s = 0.f;
+  for (int c = 0; c < kChunks; ++c) s += partial[(size_t)c * len + i];
+  out[i] = s;
+}
+
+// Fixed-order block sum of kThreads values.
+__device__ float block_sum(float v, float *red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  const float r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ float misfit_of(const float *yb, float *red) {
+  float s = 0.f;
+  for (int p = threadIdx.x; p < kP; p += kThreads) s += yb[3 * kP + p];
+  return block_sum(s, red);
+}
+
+// Loss = w_m mean_b (m - m*)^2 + w_g mean_{b,c,p} (g - g*)^2 and its
+// gradient with respect to the last layer's output.
+__global__ void __launch_bounds__(kThreads) head_loss(int batch, const float *__restrict__ y4,
+                                                      const float *__restrict__ m_true,
+                                                      const float *__restrict__ g_true, float w_m,
+                                                      float w_g, float *__restrict__ dy4,
+                                                      double *__restrict__ loss_part) {
+  __shared__ float red[kThreads];
+  const int b = blockIdx.x;
+  const float *yb = y4 + (size_t)b * 4 * kP;
+  const float m = misfit_of(yb, red);
+  const float dm = m - m_true[b];
+  const float ng = (float)batch * 3 * kP;
+  float lg = 0.f;
+  for (int i = threadIdx.x; i < 3 * kP; i += kThreads) {
+    const float diff = yb[i] - g_true[(size_t)b * 3 * kP + i];
+    lg += diff * diff;
+    dy4[(size_t)b * 4 * kP + i] = 2.f * w_g * diff / ng;
+  }
+  for (int p = threadIdx.x; p < kP; p += kThreads)
+    dy4[(size_t)b * 4 * kP + 3 * kP + p] = 2.f * w_m * dm / (float)batch;
+  lg = block_sum(lg, red);
+  if (threadIdx.x == 0)
+    loss_part[b] = (double)w_m * dm * dm / batch + (double)w_g * lg / ng;
+}
+
+__global__ void sum_loss(int n, const double *__restrict__ part, double *__restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += part[i];
+    *out = s;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) head_predict(const float *__restrict__ y4,
+                                                         float *__restrict__ misfit,
+                                                         float *__restrict__ grad) {
+  __shared__ float red[kThreads];
+  const int b = blockIdx.x;
+  const float *yb = y4 + (size_t)b * 4 * kP;
+  const float m = misfit_of(yb, red);
+  for (int i = threadIdx.x; i < 3 * kP; i += kThreads) grad[(size_t)b * 3 * kP + i] = yb[i];
+  if (threadIdx.x == 0) misfit[b] = m;
+}
+
+__global__ void adam_step(size_t n, float *__restrict__ p, const float *__restrict__ g,
+                          float *__restrict__ m, float *__restrict__ v,
+                          __nv_bfloat16 *__restrict__ wbf, float lr, float b1, float b2, float eps,
+                          float bc1, float bc2) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float pi = p[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  p[i] = pi;
+  wbf[i] = __float2bfloat16_rn(pi);
+}
+
+__global__ void to_bf16(size_t n, const float *__restrict__ p, __nv_bfloat16 *__restrict__ wbf) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) wbf[i] = __float2bfloat16_rn(p[i]);
+}
+
+unsigned blocks(size_t n, int t = 256) { return static_cast<unsigned>((n + t - 1) / t); }
+
+void check(cudaError_t e, const char *what) { cuda_check(e, what); }
+
+void configure_once(int device) {
+  static unsigned long long done = 0;
+  const unsigned long long bit = 1ull << (device & 63);
+  if (done & bit) return;
+  const int smem = static_cast<int>(conv_smem());
+  check(cudaFuncSetAttribute(conv_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+        "conv smem");
+  check(cudaFuncSetAttribute(conv_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+        "conv smem");
+  check(cudaFuncSetAttribute(conv_backward_data, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+        "conv smem");
+  check(cudaFuncSetAttribute(conv_backward_weight, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem),
+        "conv smem");
+  done |= bit;
+}
+
+}  // namespace
+
+size_t weight_offset(int layer) {
+  size_t off = 0;
+  for (int l = 0; l < layer; ++l) off += layer_size(l);
+  return off;
+}
+
+size_t bias_offset(int layer) { return weight_offset(layer) + (size_t)kCout[layer] * kCin[layer] * 9; }
+
+size_t num_params() { return weight_offset(kLayers); }
+
+Net::Net(int device, int max_batch) : device_(device), max_batch_(max_batch) {
+  if (max_batch <= 0) throw Error(PSV_ERR_INVALID_ARGUMENT, "max_batch must be positive");
+  DeviceGuard guard(device_);
+  check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  configure_once(device_);
+  const size_t n = num_params();
+  params_.allocate(n * sizeof(float));
+  wbf_.allocate(n * sizeof(__nv_bfloat16));
+  grads_.allocate(n * sizeof(float));
+  adam_m_.allocate(n * sizeof(float));
+  adam_v_.allocate(n * sizeof(float));
+  size_t maxlen = 0;
+  for (int l = 0; l < kLayers; ++l) maxlen = std::max(maxlen, layer_size(l));
+  partials_.allocate(kChunks * maxlen * sizeof(float));
+  for (int l = 0; l < kLayers; ++l)
+    act_[l].allocate((size_t)max_batch * kCout[l] * kP * sizeof(float));
+  for (auto &d : dact_) d.allocate((size_t)max_batch * kMaxC * kP * sizeof(float));
+  loss_partials_.allocate((size_t)max_batch * sizeof(double));
+  loss_.allocate(sizeof(double));
+}
+
+Net::~Net() {
+  if (stream_) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device_);
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+    cudaSetDevice(prev);
+  }
+}
+
+void Net::check_batch(int batch) const {
+  if (batch <= 0 || batch > max_batch_)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "batch must be in [1, max_batch]");
+}
+
+void Net::refresh_bf16() {
+  const size_t n = num_params();
+  to_bf16<<<blocks(n), 256, 0, stream_>>>(n, params_.as<float>(), wbf_.as<__nv_bfloat16>());
+  check(cudaGetLastError(), "to_bf16");
+}
+
+void Net::set_params(const float *host) {
+  DeviceGuard guard(device_);
+  const size_t n = num_params();
+  check(cudaMemcpyAsync(params_.get(), host, n * sizeof(float), cudaMemcpyHostToDevice, stream_),
+        "set params");
+  check(cudaMemsetAsync(adam_m_.get(), 0, n * sizeof(float), stream_), "adam");
+  check(cudaMemsetAsync(adam_v_.get(), 0, n * sizeof(float), stream_), "adam");
+  step_ = 0;
+  refresh_bf16();
+  check(cudaStreamSynchronize(stream_), "set params");
+}
+
+void Net::get_params(float *host) {
+  DeviceGuard guard(device_);
+  check(cudaMemcpyAsync(host, params_.get(), num_params() * sizeof(float), cudaMemcpyDeviceToHost,
+                        stream_),
+        "get params");
+  check(cudaStreamSynchronize(stream_), "get params");
+}
+
+void Net::forward(int batch, const float *x) {
+  const float *in = x;
+  const size_t smem = conv_smem();
+  for (int l = 0; l < kLayers; ++l) {
+    const dim3 grid(batch, (kCout[l] + kBlk - 1) / kBlk);
+    const __nv_bfloat16 *w = wbf_.as<__nv_bfloat16>() + weight_offset(l);
+    const float *bias = params_.as<float>() + bias_offset(l);
+    float *out = act_[l].as<float>();
+    if (l + 1 < kLayers)
+      conv_forward<true><<<grid, kThreads, smem, stream_>>>(kCin[l], kCout[l], kDil[l], in, w, bias,
+                                                           out);
+    else
+      conv_forward<false><<<grid, kThreads, smem, stream_>>>(kCin[l], kCout[l], kDil[l], in, w,
+                                                            bias, out);
+    check(cudaGetLastError(), "conv forward");
+    in = out;
+  }
+}
+
+double Net::backward(int batch, const float *x, const float *m_true, const float *g_true,
+                     float w_misfit, float w_grad) {
+  const size_t smem = conv_smem();
+  float *cur = dact_[0].as<float>(), *other = dact_[1].as<float>();
+  head_loss<<<batch, kThreads, 0, stream_>>>(batch, act_[kLayers - 1].as<float>(), m_true, g_true,
+                                             w_misfit, w_grad, cur, loss_partials_.as<double>());
+  sum_loss<<<1, 32, 0, stream_>>>(batch, loss_partials_.as<double>(), loss_.as<double>());
+  check(cudaGetLastError(), "head loss");
+  for (int l = kLayers - 1; l >= 0; --l) {
+    const float *in = l == 0 ? x : act_[l - 1].as<float>();
+    conv_backward_weight<<<dim3(kCout[l], kChunks), kThreads, smem, stream_>>>(
+        batch, kCin[l], kCout[l], kDil[l], in, cur, partials_.as<float>());
+    const size_t len = layer_size(l);
+    sum_chunks<<<blocks(len), 256, 0, stream_>>>(len, partials_.as<float>(),
+                                                 grads_.as<float>() + weight_offset(l));
+    check(cudaGetLastError(), "conv backward weight");
+    if (l > 0) {
+      const dim3 grid(batch, (kCin[l] + kBlk - 1) / kBlk);
+      conv_backward_data<<<grid, kThreads, smem, stream_>>>(
+          kCin[l], kCout[l], kDil[l], cur, wbf_.as<__nv_bfloat16>() + weight_offset(l),
+          act_[l - 1].as<float>(), other);
+      check(cudaGetLastError(), "conv backward data");
+      std::swap(cur, other);
+    }
+  }
+  double loss = 0;
+  check(cudaMemcpyAsync(&loss, loss_.get(), sizeof(double), cudaMemcpyDeviceToHost, stream_),
+        "loss");
+  check(cudaStreamSynchronize(stream_), "backward");
+  return loss;
+}
+
+void Net::predict(int batch, const float *x, float *misfit, float *grad) {
+  check_batch(batch);
+  DeviceGuard guard(device_);
+  forward(batch, x);
+  head_predict<<<batch, kThreads, 0, stream_>>>(act_[kLayers - 1].as<float>(), misfit, grad);
+  check(cudaGetLastError(), "head predict");
+  check(cudaStreamSynchronize(stream_), "predict");
+}
+
+double Net::loss_grad(int batch, const float *x, const float *m_true, const float *g_true,
+                      float w_misfit, float w_grad, float *dparams_host) {
+  check_batch(batch);
+  DeviceGuard guard(device_);
+  forward(batch, x);
+  const double loss = backward(batch, x, m_true, g_true, w_misfit, w_grad);
+  if (dparams_host) {
+    check(cudaMemcpyAsync(dparams_host, grads_.get(), num_params() * sizeof(float),
+                          cudaMemcpyDeviceToHost, stream_),
+          "grads");
+    check(cudaStreamSynchronize(stream_), "grads");
+  }
+  return loss;
+}
+
+double Net::train_step(int batch, const float *x, const float *m_true, const float *g_true,
+                       float w_misfit, float w_grad, const Adam &opt) {
+  check_batch(batch);
+  DeviceGuard guard(device_);
+  forward(batch, x);
+  const double loss = backward(batch, x, m_true, g_true, w_misfit, w_grad);
+  ++step_;
+  const float bc1 = 1.f - std::pow(opt.beta1, (float)step_);
+  const float bc2 = 1.f - std::pow(opt.beta2, (float)step_);
+  const size_t n = num_params();
+  adam_step<<<blocks(n), 256, 0, stream_>>>(n, params_.as<float>(), grads_.as<float>(),
+                                            adam_m_.as<float>(), adam_v_.as<float>(),
+                                            wbf_.as<__nv_bfloat16>(), opt.lr, opt.beta1, opt.beta2,
+                                            opt.eps, bc1, bc2);
+  check(cudaGetLastError(), "adam");
+  return loss;
+}
+
+}  // namespace cnn
+
+// ---- coarse-to-grid map ---------------------------------------------------
+
+namespace {
+
+__global__ void coarse_to_fields(int batch, int nx, int nz, int ncx, int ncz,
+                                 const int *__restrict__ x0, const int *__restrict__ x1,
+                                 const double *__restrict__ wx, const int *__restrict__ z0,
+                                 const int *__restrict__ z1, const double *__restrict__ wz,
+                                 const double *__restrict__ mean, const double *__restrict__ sigma,
+                                 const float *__restrict__ z, double *__restrict__ fields) {
+  const size_t n = (size_t)batch * 3 * nx * nz;
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int iz = (int)(i % nz);
+  const int ix = (int)((i / nz) % nx);
+  const int c = (int)((i / ((size_t)nx * nz)) % 3);
+  const int b = (int)(i / ((size_t)3 * nx * nz));
+  const size_t cb = (size_t)c * ncx * ncz;
+  const float *zb = z + (size_t)b * 3 * ncx * ncz + cb;
+  auto theta = [&](int a, int d) {
+    const size_t k = (size_t)a * ncz + d;
+    return mean[cb + k] + sigma[cb + k] * (double)zb[k];
+  };
+  const double fx = wx[ix], fz = wz[iz];
+  const int a0 = x0[ix], a1 = x1[ix], d0 = z0[iz], d1 = z1[iz];
+  fields[i] = (1.0 - fx) * ((1.0 - fz) * theta(a0, d0) + fz * theta(a0, d1)) +
+              fx * ((1.0 - fz) * theta(a1, d0) + fz * theta(a1, d1));
+}
+
+__global__ void fields_to_coarse(int nx, int nz, int ncx, int ncz, const int *__restrict__ x0,
+                                 const int *__restrict__ x1, const double *__restrict__ wx,
+                                 const int *__restrict__ z0, const int *__restrict__ z1,
+                                 const double *__restrict__ wz, const int *__restrict__ xs,
+                                 const int *__restrict__ xe, const int *__restrict__ zs,
+                                 const int *__restrict__ ze, const double *__restrict__ sigma,
+                                 double scale, const double *__restrict__ g,
+                                 float *__restrict__ gz) {
+  const int bc = blockIdx.x;  // b * 3 + c
+  const int c = bc % 3;
+  const double *gb = g + (size_t)bc * nx * nz;
+  for (int k = threadIdx.x; k < ncx * ncz; k += blockDim.x) {
+    const int a = k / ncz, d = k - a * ncz;
+    double acc = 0;
+    for (int ix = xs[a]; ix < xe[a]; ++ix) {
+      const double ax = (x0[ix] == a ? 1.0 - wx[ix] : 0.0) + (x1[ix] == a ? wx[ix] : 0.0);
+      if (ax == 0.0) continue;
+      double row = 0;
+      for (int iz = zs[d]; iz < ze[d]; ++iz) {
+        const double az = (z0[iz] == d ? 1.0 - wz[iz] : 0.0) + (z1[iz] == d ? wz[iz] : 0.0);
+        row += az * gb[(size_t)ix * nz + iz];
+      }
+      acc += ax * row;
+    }
+    gz[(size_t)bc * ncx * ncz + k] =
+        (float)(scale * sigma[(size_t)c * ncx * ncz + k] * acc);
+  }
+}
+
+// 1-D interpolation weights and supports along one axis of n fine points
+// (np boundary frames each side) over nc coarse nodes.
+void axis_weights(int n, int np, int nc, std::vector<int> &i0, std::vector<int> &i1,
+                  std::vector<double> &w, std::vector<int> &s, std::vector<int> &e) {
+  const int inner = n - 2 * np;
+  const double f = static_cast<double>(inner) / nc;
+  i0.resize(n);
+  i1.resize(n);
+  w.resize(n);
+  s.assign(nc, n);
+  e.assign(nc, 0);
+  for (int x = 0; x < n; ++x) {
+    const int xi = std::min(std::max(x - np, 0), inner - 1);
+    double u = (xi + 0.5) / f - 0.5;
+    u = std::min(std::max(u, 0.0), static_cast<double>(nc - 1));
+    int a = static_cast<int>(std::floor(u));
+    a = std::min(a, nc - 1);
+    i0[x] = a;
+    i1[x] = std::min(a + 1, nc - 1);
+    w[x] = u - a;
+    for (int k : {i0[x], i1[x]}) {
+      s[k] = std::min(s[k], x);
+      e[k] = std::max(e[k], x + 1);
+    }
+  }
+}
+
+template <class V>
+void upload(DeviceBuffer &d, const V &v) {
+  d.allocate(std::max<size_t>(v.size(), 1) * sizeof(v[0]));
+  if (!v.empty())
+    cuda_check(cudaMemcpy(d.get(), v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice),
+               "upload coarse map");
+}
+
+}  // namespace
+
+CoarseMap::CoarseMap(int device, int nx_, int nz_, int np_, int ncx_, int ncz_, const double *mean,
+                     const double *sigma)
+    : nx(nx_), nz(nz_), np(np_), ncx(ncx_), ncz(ncz_), device_(device) {
+  if (nx <= 2 * np || nz <= 2 * np || ncx <= 0 || ncz <= 0 || ncx > nx - 2 * np ||
+      ncz > nz - 2 * np)
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "coarse grid does not fit the inner grid");
+  DeviceGuard guard(device_);
+  std::vector<int> x0, x1, xs, xe, z0, z1, zs, ze;
+  std::vector<double> wx, wz;
+  axis_weights(nx, np, ncx, x0, x1, wx, xs, xe);
+  axis_weights(nz, np, ncz, z0, z1, wz, zs, ze);
+  upload(x0_, x0);
+  upload(x1_, x1);
+  upload(wx_, wx);
+  upload(z0_, z0);
+  upload(z1_, z1);
+  upload(wz_, wz);
+  upload(xs_, xs);
+  upload(xe_, xe);
+  upload(zs_, zs);
+  upload(ze_, ze);
+  const size_t n = (size_t)3 * ncx * ncz;
+  upload(mean_, std::vector<double>(mean, mean + n));
+  upload(sigma_, std::vector<double>(sigma, sigma + n));
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+}
+
+CoarseMap::~CoarseMap() {
+  if (stream_) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device_);
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+    cudaSetDevice(prev);
+  }
+}
+
+void CoarseMap::to_fields(int batch, const float *z, double *fields, cudaStream_t s) const {
+  DeviceGuard guard(device_);
+  const size_t n = (size_t)batch * 3 * nx * nz;
+  if (!n) return;
+  cudaStream_t use = s ? s : stream_;
+  coarse_to_fields<<<static_cast<unsigned>((n + 255) / 256), 256, 0, use>>>(
+      batch, nx, nz, ncx, ncz, x0_.as<int>(), x1_.as<int>(), wx_.as<double>(), z0_.as<int>(),
+      z1_.as<int>(), wz_.as<double>(), mean_.as<double>(), sigma_.as<double>(), z, fields);
+  cuda_check(cudaGetLastError(), "coarse to fields");
+  if (!s) cuda_check(cudaStreamSynchronize(stream_), "coarse to fields");
+}
+
+void CoarseMap::gradient(int batch, const double *gfields, float *gz, double scale,
+                         cudaStream_t s) const {
+  DeviceGuard guard(device_);
+  if (batch <= 0) return;
+  cudaStream_t use = s ? s : stream_;
+  fields_to_coarse<<<batch * 3, 256, 0, use>>>(nx, nz, ncx, ncz, x0_.as<int>(), x1_.as<int>(),
+                                               wx_.as<double>(), z0_.as<int>(), z1_.as<int>(),
+                                               wz_.as<double>(), xs_.as<int>(), xe_.as<int>(),
+                                               zs_.as<int>(), ze_.as<int>(), sigma_.as<double>(),
+                                               scale, gfields, gz);
+  cuda_check(cudaGetLastError(), "fields to coarse");
+  if (!s) cuda_check(cudaStreamSynchronize(stream_), "fields to coarse");
+}
+
+}  // namespace psv

@@ -25,22 +25,6 @@ namespace {
 constexpr double kRefPi = 3.14159265;
 constexpr double kMPi = 3.14159265358979323846;
 
-class DeviceGuard {
- public:
-  explicit DeviceGuard(int device) {
-    cudaGetDevice(&prev_);
-    if (prev_ != device) cuda_check(cudaSetDevice(device), "cudaSetDevice");
-    restore_ = prev_ != device;
-  }
-  ~DeviceGuard() {
-    if (restore_) cudaSetDevice(prev_);
-  }
-
- private:
-  int prev_ = 0;
-  bool restore_ = false;
-};
-
 std::string pad5(int n) {
   std::ostringstream ss;
   ss << std::setw(5) << std::setfill('0') << n;

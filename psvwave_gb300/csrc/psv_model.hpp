@@ -18,6 +18,28 @@
 
 namespace psv {
 
+// Throws Error(PSV_ERR_CUDA) with the CUDA message when e is not cudaSuccess.
+void cuda_check(cudaError_t e, const char *what);
+
+// Makes `device` current for the scope and restores the previous device.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    cudaGetDevice(&prev_);
+    if (prev_ != device) cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    restore_ = prev_ != device;
+  }
+  ~DeviceGuard() {
+    if (restore_) cudaSetDevice(prev_);
+  }
+  DeviceGuard(const DeviceGuard &) = delete;
+  DeviceGuard &operator=(const DeviceGuard &) = delete;
+
+ private:
+  int prev_ = 0;
+  bool restore_ = false;
+};
+
 // Owning device allocation.
 class DeviceBuffer {
  public:
@@ -52,9 +74,6 @@ class DeviceBuffer {
   void *ptr_ = nullptr;
   size_t bytes_ = 0;
 };
-
-// Throws Error(PSV_ERR_CUDA) when e is not cudaSuccess.
-void cuda_check(cudaError_t e, const char *what);
 
 class Batch;
 

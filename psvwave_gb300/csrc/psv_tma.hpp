@@ -63,11 +63,13 @@ bool encode_input_maps(Maps &m, const fast::Fields &in, const float *lm, const f
 void append_tiles(int cfg, int sim, int nx, int nz, std::vector<int4> &tiles);
 
 // One time step of every simulation in `sims` (device table), over the
-// tiles in `tiles` (device, n_tiles entries). parity p: inputs in set p,
-// outputs in set 1 - p. store: forward snapshots at steps it % si == 0.
-// *err is raised when a CTA's bounded wait for its copies times out.
-cudaError_t step(const SimDesc *sims, const int4 *tiles, int n_tiles, int cfg, bool adjoint,
-                 int it, int parity, bool store, int *err, cudaStream_t s);
+// tiles in `tiles` (device, n_tiles entries); with `active` (device, one
+// flag per simulation) non-null, only simulations flagged non-zero step.
+// parity p: inputs in set p, outputs in set 1 - p. store: forward snapshots
+// at steps it % si == 0. *err is raised when a CTA's bounded wait for its
+// copies times out.
+cudaError_t step(const SimDesc *sims, const int4 *tiles, int n_tiles, const int *active, int cfg,
+                 bool adjoint, int it, int parity, bool store, int *err, cudaStream_t s);
 
 // The same step for one simulation whose descriptor `desc` goes out whole
 // as a kernel parameter; tiles follow from the grid.

@@ -446,12 +446,14 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
                          err);
 }
 
-// Many simulations: tile table entries (sim, x0, z0, first) per CTA.
+// Many simulations: tile table entries (sim, x0, z0, first) per CTA. With
+// `active` non-null, the CTAs of simulations whose flag is 0 return at once.
 template <class S, int CFG, bool ADJ>
 __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
     fused_step_tma_batch(const SimDesc *__restrict__ sims, const int4 *__restrict__ tiles,
-                         int it, int parity, int store, int *err) {
+                         const int *__restrict__ active, int it, int parity, int store, int *err) {
   const int4 t = tiles[blockIdx.x];
+  if (active && !active[t.x]) return;
   const SimDesc &d = sims[t.x];
   step_body<S, CFG, ADJ>(d, d.maps[parity], t.y, t.z, t.w != 0, it, parity, store, err);
 }
@@ -472,14 +474,14 @@ cudaError_t configure(K kernel, int smem, unsigned long long &configured) {
 }
 
 template <class S, int CFG, bool ADJ>
-cudaError_t launch(const SimDesc *sims, const int4 *tiles, int n_tiles, int it, int parity,
-                   int store, int *err, cudaStream_t s) {
+cudaError_t launch(const SimDesc *sims, const int4 *tiles, int n_tiles, const int *active, int it,
+                   int parity, int store, int *err, cudaStream_t s) {
   static unsigned long long configured = 0;
   cudaError_t e = configure(fused_step_tma_batch<S, CFG, ADJ>, S::SMEM, configured);
   if (e != cudaSuccess) return e;
   if (n_tiles <= 0) return cudaSuccess;
-  fused_step_tma_batch<S, CFG, ADJ><<<n_tiles, S::NT, S::SMEM, s>>>(sims, tiles, it, parity,
-                                                                    store, err);
+  fused_step_tma_batch<S, CFG, ADJ><<<n_tiles, S::NT, S::SMEM, s>>>(sims, tiles, active, it,
+                                                                    parity, store, err);
   return cudaGetLastError();
 }
 
@@ -597,14 +599,16 @@ cudaError_t step_single(const SimDesc &d, int cfg, bool adjoint, int it, int par
                  : launch_single<Big, kTile32x60, false>(d, it, parity, st, err, s);
 }
 
-cudaError_t step(const SimDesc *sims, const int4 *tiles, int n_tiles, int cfg, bool adjoint,
-                 int it, int parity, bool store, int *err, cudaStream_t s) {
+cudaError_t step(const SimDesc *sims, const int4 *tiles, int n_tiles, const int *active, int cfg,
+                 bool adjoint, int it, int parity, bool store, int *err, cudaStream_t s) {
   const int st = store ? 1 : 0;
+  const int *a = active;
   if (cfg == kTile16x28)
-    return adjoint ? launch<Small, kTile16x28, true>(sims, tiles, n_tiles, it, parity, st, err, s)
-                   : launch<Small, kTile16x28, false>(sims, tiles, n_tiles, it, parity, st, err, s);
-  return adjoint ? launch<Big, kTile32x60, true>(sims, tiles, n_tiles, it, parity, st, err, s)
-                 : launch<Big, kTile32x60, false>(sims, tiles, n_tiles, it, parity, st, err, s);
+    return adjoint ? launch<Small, kTile16x28, true>(sims, tiles, n_tiles, a, it, parity, st, err, s)
+                   : launch<Small, kTile16x28, false>(sims, tiles, n_tiles, a, it, parity, st, err,
+                                                      s);
+  return adjoint ? launch<Big, kTile32x60, true>(sims, tiles, n_tiles, a, it, parity, st, err, s)
+                 : launch<Big, kTile32x60, false>(sims, tiles, n_tiles, a, it, parity, st, err, s);
 }
 
 }  // namespace tma

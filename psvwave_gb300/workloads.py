@@ -176,3 +176,32 @@ def c3_media(params=None, seed=3):
     true = (vp, vs, rho)
     start = tuple(gaussian_smooth(a, 20.0) for a in true)
     return true, start
+
+
+def c4_params(nt=2000, peak_frequency=15.0):
+    """The surrogate Monte Carlo workload: the c0 grid (200 x 100 inner
+    cells, 25-cell boundary, dx = dz = 1.249) with dt = 2e-4 (c0's 2.5e-4
+    is reduced so that prior draws 4 sigma above the mean stay inside the CFL
+    limit), nt = 2000; c0's two sources (45 and 60 degrees) fired together
+    without delay, 19 receivers along z = 10. The Ricker wavelet peaks at
+    15 Hz: a 10 % velocity change shifts the two-way travel time through the
+    model by about 12 ms, under the 33 ms half-period, so prior draws stay
+    within half a cycle of the data (at c0's 50 Hz they would not)."""
+    p = c0_params()
+    p.update(nt=nt, dt=2e-4, delay_cycles_per_shot=0, snapshot_interval=10,
+             peak_frequency=peak_frequency)
+    return p
+
+
+C4_COARSE = (20, 10)
+
+
+def c4_prior():
+    """Mean and standard deviation [3][20][10] of the coarse parameters (vp,
+    vs, rho): a layered mean, vp from 1600 m/s at the top coarse row to 2200
+    m/s at the bottom, vs = 0.45 vp, rho = 310 vp^0.25 (Gardner); sigma =
+    10 % of the mean."""
+    ncx, ncz = C4_COARSE
+    vp = np.repeat((1600.0 + 600.0 * np.arange(ncz) / (ncz - 1))[None, :], ncx, axis=0)
+    mean = np.stack([vp, 0.45 * vp, 310.0 * vp ** 0.25])
+    return mean, 0.1 * mean

@@ -16,8 +16,11 @@ from tests.conftest import NB2_INI, ROOT, SMALL_INI
 
 
 def declared_functions():
-    text = open(os.path.join(ROOT, "include", "psvwave.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(psv_\w+)\s*\(", text, re.M)))
+    names = set()
+    for header in ("psvwave.h", "psvwave_surrogate.h"):
+        text = open(os.path.join(ROOT, "include", header)).read()
+        names |= set(re.findall(r"^\s*(?:int|const char \*)\s*(psv_\w+)\s*\(", text, re.M))
+    return sorted(names)
 
 
 def test_library_exports_every_declared_function():
