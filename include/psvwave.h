@@ -267,6 +267,11 @@ int psv_autotune(psv_model *m, int n_steps, int *chosen);
  * (host) or psv_get_exact_gradient_device. psv_exact_bytes estimates the
  * device memory of a given checkpoint interval. */
 int psv_exact_gradient(psv_model *m, int checkpoint_every, double *misfit);
+/* The same over the listed shots only (each at most once): their misfit and
+ * gradient, the per-rank part of a gradient sharded by shot across GPUs
+ * (shots are independent, src/fdModel.cpp:1293-1305). */
+int psv_exact_gradient_shots(psv_model *m, int checkpoint_every, const int *shots, int n,
+                             double *misfit);
 int psv_get_exact_gradient(psv_model *m, double *g_vp, double *g_vs, double *g_rho);
 int psv_get_exact_gradient_device(psv_model *m, double *g_vp, double *g_vs, double *g_rho);
 int psv_exact_bytes(const psv_model *m, int checkpoint_every, size_t *bytes);

@@ -117,6 +117,7 @@ _SIGNATURES = {
     "psv_get_tile_shape": [_vp, _ip],
     "psv_autotune": [_vp, _c_int, _ip],
     "psv_exact_gradient": [_vp, _c_int, _dp],
+    "psv_exact_gradient_shots": [_vp, _c_int, _ip, _c_int, _dp],
     "psv_get_exact_gradient": [_vp, _dp, _dp, _dp],
     "psv_get_exact_gradient_device": [_vp, _vp, _vp, _vp],
     "psv_exact_bytes": [_vp, _c_int, ctypes.POINTER(ctypes.c_size_t)],

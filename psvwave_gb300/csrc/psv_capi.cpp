@@ -551,6 +551,16 @@ int psv_exact_gradient(psv_model *m, int checkpoint_every, double *misfit) {
   });
 }
 
+int psv_exact_gradient_shots(psv_model *m, int checkpoint_every, const int *shots, int n,
+                             double *misfit) {
+  return guarded([&] {
+    if (n < 0) throw psv::Error(PSV_ERR_INVALID_ARGUMENT, "n must not be negative");
+    if (n) need(shots, "shots");
+    const double v = M(m).exact_gradient(checkpoint_every, std::vector<int>(shots, shots + n));
+    if (misfit) *misfit = v;
+  });
+}
+
 int psv_get_exact_gradient(psv_model *m, double *g_vp, double *g_vs, double *g_rho) {
   return guarded([&] { M(m).get_exact_gradient(g_vp, g_vs, g_rho, false); });
 }

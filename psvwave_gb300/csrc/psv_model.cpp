@@ -463,7 +463,20 @@ size_t Model::exact_bytes(int C) const {
 }
 
 double Model::exact_gradient(int C) {
+  std::vector<int> all(cfg_.n_shots);
+  for (int s = 0; s < cfg_.n_shots; ++s) all[s] = s;
+  return exact_gradient(C, all);
+}
+
+double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
   DeviceGuard guard(device_);
+  {
+    std::vector<char> seen(cfg_.n_shots, 0);
+    for (int s : shot_list) {
+      if (s < 0 || s >= cfg_.n_shots) throw Error(PSV_ERR_INVALID_ARGUMENT, "i_shot out of range");
+      if (seen[s]++) throw Error(PSV_ERR_INVALID_ARGUMENT, "a shot is listed twice");
+    }
+  }
   const int nt = cfg_.nt, n_shots = cfg_.n_shots, nr = cfg_.nr;
   if (C <= 0 || C > nt) C = nt;
   const int n_ck = (nt + C - 1) / C;
@@ -663,8 +676,30 @@ double Model::exact_gradient(int C) {
     }
   };
   cur_ = 0;
-  for (int shot = 0; shot < n_shots; ++shot) run_loop(2, shot, false, C, [&] { one_shot(shot); });
-  const double misfit = calculate_l2_misfit();
+  for (int shot : shot_list) run_loop(2, shot, false, C, [&] { one_shot(shot); });
+  double misfit = 0;
+  if (static_cast<int>(shot_list.size()) == n_shots) {
+    misfit = calculate_l2_misfit();
+  } else {
+    // Misfit of the listed shots: the same reduction over each shot's slice.
+    const size_t per = static_cast<size_t>(nr) * nt;
+    for (int shot : shot_list) {
+      if (!per) break;
+      const size_t off = static_cast<size_t>(shot) * per;
+      int parts = static_cast<int>(std::min<size_t>(kPartials, (per + 255) / 256));
+      if (parts < 1) parts = 1;
+      cuda_check(misfit_l2(per, cfg_.dt, rtf_true_[0].as<double>() + off, rtf_[0].as<double>() + off,
+                           rtf_true_[1].as<double>() + off, rtf_[1].as<double>() + off,
+                           partials_.as<double>(), parts, scalar_.as<double>(), s),
+                 "shot misfit");
+      double v = 0;
+      cuda_check(cudaMemcpyAsync(&v, scalar_.get(), sizeof(double), cudaMemcpyDeviceToHost, s),
+                 "misfit copy");
+      synchronize();
+      misfit += v;
+    }
+    misfit_ = misfit;
+  }
   // Chain rule to (vp, vs, rho).
   cuda_check(exact_chain(g, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(),
                          gex_[0].as<double>(), gex_[1].as<double>(), gex_[2].as<double>(),

@@ -153,6 +153,9 @@ class Model {
   // one segment, every state kept). Returns the misfit; the gradient stays on
   // the device (get_exact_gradient).
   double exact_gradient(int checkpoint_every);
+  // The same over the listed shots only (misfit and gradient of those
+  // shots): the per-rank part of a shot-sharded gradient.
+  double exact_gradient(int checkpoint_every, const std::vector<int> &shots);
   void get_exact_gradient(double *g_vp, double *g_vs, double *g_rho, bool device_pointers);
   size_t exact_bytes(int checkpoint_every) const;
   int variant() const { return variant_; }

@@ -234,14 +234,22 @@ class fdModel:
         self.run_model(verbose=verbose, simulate_adjoint=True)
         return self.misfit, self.get_gradient_vector()
 
-    def exact_gradient(self, checkpoint_every=100, on_device=False):
+    def exact_gradient(self, checkpoint_every=100, on_device=False, shots=None):
         """Misfit and its gradient with respect to (vp, vs, rho) over all
-        shots by the exact discrete adjoint (the transpose of the time
-        stepping), with forward states rebuilt from checkpoints every
-        `checkpoint_every` steps. Returns (misfit, (g_vp, g_vs, g_rho)),
-        numpy arrays, or CUDA tensors with on_device=True."""
+        shots (or the listed `shots`) by the exact discrete adjoint (the
+        transpose of the time stepping), with forward states rebuilt from
+        checkpoints every `checkpoint_every` steps. Returns (misfit,
+        (g_vp, g_vs, g_rho)), numpy arrays, or CUDA tensors with
+        on_device=True."""
         mis = ctypes.c_double()
-        _capi.check(self._lib.psv_exact_gradient(self._h, int(checkpoint_every), ctypes.byref(mis)))
+        if shots is None:
+            _capi.check(self._lib.psv_exact_gradient(self._h, int(checkpoint_every),
+                                                     ctypes.byref(mis)))
+        else:
+            s = np.ascontiguousarray(np.asarray(shots, dtype=np.int32).reshape(-1))
+            _capi.check(self._lib.psv_exact_gradient_shots(
+                self._h, int(checkpoint_every), s.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                int(s.size), ctypes.byref(mis)))
         if on_device:
             self._info.misfit = mis.value
             return mis.value, self.get_exact_gradient_device()

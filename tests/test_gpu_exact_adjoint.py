@@ -125,3 +125,16 @@ def test_exact_gradient_graph_replay_is_bitwise(golden, precision):
         assert mis == runs[0][0]
         for a, b in zip(g, runs[0][1]):
             assert np.array_equal(a, b)
+
+
+def test_exact_gradient_of_shot_subsets_adds_up(golden):
+    # The per-rank part of a shot-sharded gradient: shot subsets add up to
+    # the all-shot gradient and misfit.
+    m = setup(golden, "fp64")
+    mis, g = m.exact_gradient(40)
+    parts = [m.exact_gradient(40, shots=[s]) for s in range(m.n_shots)]
+    assert abs(sum(p[0] for p in parts) - mis) <= 1e-12 * abs(mis)
+    for k in range(3):
+        assert rel_l2(sum(p[1][k] for p in parts), g[k]) <= 1e-12
+    with pytest.raises(ValueError):
+        m.exact_gradient(40, shots=[0, 0])
