@@ -249,12 +249,12 @@ def fwi_gradients_c3(steps):
 def mc_samples_c4():
     """Accepted MC samples/s on the surrogate workload (c0 grid, 600 coarse
     parameters): delayed-acceptance HMC screened by the trained network
-    (2048 prior triples + 512 local triples here; python -m
+    (4096 prior triples + 512 local triples here; python -m
     psvwave_gb300.c4 runs the full 20000), against HMC with the solver's
     exact gradients and against screening by the prior alone."""
     from psvwave_gb300 import c4
 
-    out = c4.run(n_train=2048, n_local=512, n_chains=128, n_iter=40, plain_iter=3)
+    out = c4.run(n_train=4096, n_local=512, n_chains=128, n_iter=40, plain_iter=3)
     out["unit"] = "accepted samples/s"
     out["workload"] = ("c4: 250x150 grid, nt=2000, Ricker 15 Hz, 600 coarse parameters "
                        "(20x10 vp/vs/rho, prior sigma 10%), s2 = misfit(prior mean)/20; "

@@ -25,7 +25,7 @@ def _rel(pred, true):
 
 
 def run(n_train=2048, n_local=512, n_chains=128, n_iter=40, burn_in=20, eps=0.03, n_leap=10,
-        plain_chains=16, plain_iter=3, s2_div=20.0, epochs=60, seed=0, log=None):
+        plain_chains=16, plain_iter=3, s2_div=20.0, epochs=None, seed=0, log=None):
     """Runs the workload; returns a dict of measurements.
 
     The posterior's noise scale is s2 = misfit(prior mean) / s2_div. Chains
@@ -37,6 +37,8 @@ def run(n_train=2048, n_local=512, n_chains=128, n_iter=40, burn_in=20, eps=0.03
         if log:
             log(msg)
 
+    if epochs is None:  # about 4500 Adam steps whatever the set size, at least 60 epochs
+        epochs = max(60, (4500 * 256) // max(n_train, 1))
     out = {}
     S = sg.c4_setup(n_chains, s2=1.0)
     post = S["posterior"]
