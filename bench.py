@@ -29,7 +29,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Gcell-updates/s"
 # FP32 algorithmic bytes per cell-update of each step kernel
-BYTES_PER_CELL = {"stress_step": 48, "velocity_step": 36, "fused_step": 56, "fused_step_tma": 52}
+BYTES_PER_CELL = {"stress_step": 48, "velocity_step": 36, "fused_step": 56, "fused_step_tma": 52,
+                  "fused_steps_tma": 52}
 
 
 def parse():
@@ -436,16 +437,22 @@ def main():
     h2d = 3 * cells * 8
     d2h = 2 * model.n_shots * model.nr * model.nt * 8
 
-    # Roofline of the dominant kernel. Its average launch duration over the
-    # timed region: the region's device time divided by the time-step
-    # launches in it (each timed forward also holds one field memset and the
-    # receiver prefix sum, so the figure is slightly pessimistic). Launches
-    # of consecutive steps overlap their prologue with the previous step's
-    # tail (programmatic dependent launch). The isolated per-launch time,
-    # from CUDA events around each of 500 launches, which break that
-    # overlap, is reported beside it.
+    # Roofline of the dominant kernel, per time step: the timed region's
+    # device time divided by its time steps (each timed forward also holds
+    # one field memset and the receiver prefix sum, so the figure is
+    # slightly pessimistic), against the algorithmic bytes of one step. With
+    # one launch per step, consecutive launches overlap their prologue with
+    # the previous step's tail (programmatic dependent launch); with the
+    # persistent scheme all steps are one launch whose tiles start a step as
+    # soon as their neighbours have finished the previous one. The isolated
+    # time (CUDA events around each of 500 per-step launches, or around one
+    # 500-step persistent launch) is reported beside it.
     per_step_ms, kernel_ms = model.profile_forward(0, 500)
     dominant = max(kernel_ms, key=kernel_ms.get)
+    # Kernels of ours per timed forward: the time-step launches (all steps in
+    # one launch for the persistent scheme) and the receiver prefix sum.
+    persistent = model.kernel_variant == "fused_tma_persistent"
+    launches_per_forward = 2 if persistent else len(kernel_ms) * nt + 1
     words = 2 if args.precision == "fp64" else 1
     if dominant in ("stress_step", "velocity_step"):  # two launches per time step
         dominant = "stress_step+velocity_step"
@@ -459,6 +466,7 @@ def main():
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": measured_traffic(dominant), "bytes_per_launch": bpc * cells,
                 "kernel_avg_ms_timed_region": kernel_avg_ms,
+                "launch_scheme": model.kernel_variant,
                 "isolated_kernel_ms": kernel_ms, "isolated_step_ms": per_step_ms,
                 "achieved_gcells_per_launch": cells / (kernel_avg_ms / 1e3) / 1e9}
 
@@ -486,7 +494,7 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": (len(kernel_ms) * nt + 1) * args.steps,
+            "gpu_launches": launches_per_forward * args.steps,
             "roofline": roofline,
             "cpu_baseline": base,
             "clocks": clocks,

@@ -235,21 +235,29 @@ int psv_profile_forward(psv_model *m, int i_shot, int n_steps, double *per_step_
 const char *psv_step_kernel_name(const psv_model *m, int k);
 
 /* Time-step kernel variant: PSV_VARIANT_FUSED (one launch per step over
- * ping-pong buffers; FP32 only, the FP32 default) or PSV_VARIANT_TWO_KERNEL
- * (separate stress and velocity launches, as the reference's two loop nests;
- * the only FP64 variant) or PSV_VARIANT_FUSED_TMA (the fused step with TMA
- * tile loads; FP32, the default). Results
- * of the FP32 variants agree to FP32 rounding. No counterpart in the
- * reference. */
-enum psv_variant { PSV_VARIANT_FUSED = 0, PSV_VARIANT_TWO_KERNEL = 1, PSV_VARIANT_FUSED_TMA = 2 };
+ * ping-pong buffers; FP32 only), PSV_VARIANT_TWO_KERNEL (separate stress and
+ * velocity launches, as the reference's two loop nests; the only FP64
+ * variant), PSV_VARIANT_FUSED_TMA (the fused step with TMA tile loads, one
+ * launch per step; FP32, the default) or PSV_VARIANT_FUSED_TMA_PERSISTENT
+ * (the same step, every time step of a simulation in one persistent launch
+ * whose tiles start a step as soon as their neighbours have finished the
+ * previous one). Results of the FP32 variants agree to FP32 rounding. No
+ * counterpart in the reference. */
+enum psv_variant {
+  PSV_VARIANT_FUSED = 0,
+  PSV_VARIANT_TWO_KERNEL = 1,
+  PSV_VARIANT_FUSED_TMA = 2,
+  PSV_VARIANT_FUSED_TMA_PERSISTENT = 3
+};
 int psv_set_kernel_variant(psv_model *m, int variant);
 int psv_get_kernel_variant(const psv_model *m, int *variant);
 
 /* Tile shape of the FP32 TMA step: PSV_TILE_32X60 (x rows by z columns;
  * large grids) or PSV_TILE_16X28 (small grids; chosen by default below
- * 400,000 grid points). psv_autotune times every shape on n_steps forward
- * steps of shot 0 and keeps the fastest in *chosen. No counterpart in the
- * reference. */
+ * 400,000 grid points). psv_autotune times every tile shape with both TMA
+ * launch schemes (PSV_VARIANT_FUSED_TMA and _PERSISTENT) on n_steps forward
+ * steps of shot 0, replayed as CUDA graphs, keeps the fastest pair and
+ * returns its shape in *chosen. No counterpart in the reference. */
 enum psv_tile_shape { PSV_TILE_32X60 = 0, PSV_TILE_16X28 = 1 };
 int psv_set_tile_shape(psv_model *m, int shape);
 int psv_get_tile_shape(const psv_model *m, int *shape);

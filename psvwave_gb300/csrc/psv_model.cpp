@@ -90,7 +90,16 @@ Model::Model(const Config &cfg, int precision, int device)
   // Large grids keep the 32 x 60 tiles; small ones fill the GPU with 16 x 28.
   if (static_cast<double>(geo_.nx) * geo_.nz < 4.0e5) tile_cfg_ = tma::kTile16x28;
   build_descs();
-  if (tma_ok_) variant_ = kFusedTma;
+  if (tma_ok_) {
+    // One launch per step, or the persistent launch when a step has at least
+    // a full wave of 32 x 60 tiles (measured faster there; smaller grids are
+    // latency-bound and keep the per-step launches). autotune() times both.
+    variant_ = kFusedTma;
+    const int slots = tma::resident_ctas(tile_cfg_, false);
+    if (tile_cfg_ == tma::kTile32x60 && slots > 0 &&
+        tma::tile_count(tile_cfg_, geo_.nx, geo_.nz) >= slots)
+      variant_ = kFusedTmaPersistent;
+  }
   synchronize();
 }
 
@@ -397,6 +406,30 @@ void Model::build_descs() {
     }
     if (!tma::make_maps(d, mu_.as<float>(), tile_cfg_)) return;
   }
+  // Receivers by tile (persistent step) and the persistent step's schedule.
+  {
+    const int n_tiles = tma::tile_count(tile_cfg_, geo_.nx, geo_.nz);
+    std::vector<int> start(n_tiles + 1, 0), list(std::max(cfg_.nr, 1));
+    for (int r = 0; r < cfg_.nr; ++r)
+      ++start[1 + tma::tile_of(tile_cfg_, geo_.nz, ix_rec_[r], iz_rec_[r])];
+    for (int t = 0; t < n_tiles; ++t) start[t + 1] += start[t];
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int r = 0; r < cfg_.nr; ++r)
+      list[fill[tma::tile_of(tile_cfg_, geo_.nz, ix_rec_[r], iz_rec_[r])]++] = r;
+    rec_tile_start_.allocate(start.size() * sizeof(int));
+    rec_tile_list_.allocate(list.size() * sizeof(int));
+    cuda_check(cudaMemcpy(rec_tile_start_.get(), start.data(), start.size() * sizeof(int),
+                          cudaMemcpyHostToDevice),
+               "receiver tiles");
+    cuda_check(cudaMemcpy(rec_tile_list_.get(), list.data(), list.size() * sizeof(int),
+                          cudaMemcpyHostToDevice),
+               "receiver tiles");
+    sched_.allocate(tma::sched_words(tile_cfg_, geo_.nx, geo_.nz) * sizeof(unsigned));
+    for (int k = 0; k < n_shots; ++k) {
+      descs[k].rec_start = rec_tile_start_.as<int>();
+      descs[k].rec_list = rec_tile_list_.as<int>();
+    }
+  }
   descs_h_ = std::move(descs);
   tma_ok_ = true;
 }
@@ -415,6 +448,15 @@ cudaError_t Model::tma_forward(int shot, bool store, int it0, int it1, bool zero
   }
   const tma::SimDesc &h = descs_h_[shot];
   const int cfg = tile_cfg_;
+  if (variant_ == kFusedTmaPersistent && it1 > it0) {
+    cudaError_t e = cudaMemsetAsync(sched_.get(), 0, sched_.bytes(), s);
+    if (e == cudaSuccess)
+      e = tma::steps_persistent(h, cfg, false, it0, it1 - it0, cur_, store, err_flag_.as<int>(),
+                                sched_.as<unsigned>(), s);
+    if (e != cudaSuccess) return e;
+    cur_ ^= (it1 - it0) & 1;
+    it0 = it1;  // done; falls through to the seismograms
+  }
   for (int it = it0; it < it1; ++it) {
     cudaEvent_t *ev = events ? events + 2 * (it - it0) : nullptr;
     if (ev) cudaEventRecord(ev[0], s);
@@ -445,6 +487,15 @@ cudaError_t Model::tma_adjoint(int shot) {
   cur_ = 0;
   const tma::SimDesc &h = descs_h_[cfg_.n_shots + shot];
   const int cfg = tile_cfg_;
+  if (variant_ == kFusedTmaPersistent) {
+    cudaError_t e = cudaMemsetAsync(sched_.get(), 0, sched_.bytes(), s);
+    if (e == cudaSuccess)
+      e = tma::steps_persistent(h, cfg, true, cfg_.nt - 1, cfg_.nt, 0, false, err_flag_.as<int>(),
+                                sched_.as<unsigned>(), s);
+    if (e != cudaSuccess) return e;
+    cur_ = cfg_.nt & 1;
+    return cudaGetLastError();
+  }
   for (int it = cfg_.nt - 1; it >= 0; --it) {
     cudaError_t e = tma::step_single(h, cfg, true, it, cur_, false, err_flag_.as<int>(), s);
     if (e != cudaSuccess) return e;
@@ -523,7 +574,7 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
   // field sets (checkpoint pass) and from state slot j straight into slot
   // j + 1 (recompute), so no state is copied per step. The slots' input
   // tensor maps are encoded once per call, when first needed.
-  const bool tma = prec_ == PSV_FP32 && tma_ok_ && variant_ == kFusedTma;
+  const bool tma = prec_ == PSV_FP32 && tma_ok_ && is_tma();
   std::vector<tma::Maps> slot_maps;
   auto slot_fields = [&](int j) {
     void *p[5];
@@ -739,20 +790,41 @@ void Model::set_tile_cfg(int cfg) {
 }
 
 int Model::autotune(int n_steps) {
-  if (!(prec_ == PSV_FP32 && variant_ == kFusedTma)) return tile_cfg_;
+  if (!(prec_ == PSV_FP32 && is_tma())) return tile_cfg_;
   if (cfg_.n_shots < 1) return tile_cfg_;
-  double best = 0;
-  int best_cfg = tile_cfg_;
-  for (int c = 0; c < tma::kNumTileCfgs; ++c) {
-    set_tile_cfg(c);
-    double per_step = 0;
-    profile_forward(0, std::min(n_steps, cfg_.nt), &per_step, nullptr, 0);  // warm
-    profile_forward(0, std::min(n_steps, cfg_.nt), &per_step, nullptr, 0);
-    if (c == 0 || per_step < best) {
-      best = per_step;
-      best_cfg = c;
+  DeviceGuard guard(device_);
+  n_steps = std::max(1, std::min(n_steps, cfg_.nt));
+  // Every (launch scheme, tile shape) pair, timed as forward_simulate runs
+  // it: the time loop replayed as a CUDA graph, over n_steps steps.
+  cudaEvent_t a, b;
+  cuda_check(cudaEventCreate(&a), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&b), "cudaEventCreate");
+  float best = 0;
+  int best_cfg = tile_cfg_, best_variant = variant_;
+  bool first = true;
+  for (int v : {static_cast<int>(kFusedTma), static_cast<int>(kFusedTmaPersistent)}) {
+    for (int c = 0; c < tma::kNumTileCfgs; ++c) {
+      set_variant(v);
+      set_tile_cfg(c);
+      forward_simulate(0, false, false, false, n_steps);  // eager
+      forward_simulate(0, false, false, false, n_steps);  // captured
+      cuda_check(cudaEventRecord(a, stream()), "cudaEventRecord");
+      forward_simulate(0, false, false, false, n_steps);
+      cuda_check(cudaEventRecord(b, stream()), "cudaEventRecord");
+      cuda_check(cudaEventSynchronize(b), "cudaEventSynchronize");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      if (first || ms < best) {
+        best = ms;
+        best_cfg = c;
+        best_variant = v;
+        first = false;
+      }
     }
   }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  set_variant(best_variant);
   set_tile_cfg(best_cfg);
   return best_cfg;
 }
@@ -918,7 +990,7 @@ void Model::forward_simulate(int shot, bool store, bool verbose, bool output_wav
     cudaError_t e;
     if (prec_ == PSV_FP64)
       e = forward_f64(a, plan, shot, store, it0, it1, zero, fin, stream());
-    else if (variant_ == kFusedTma)
+    else if (is_tma())
       e = tma_forward(shot, store, it0, it1, zero, fin, nullptr);
     else if (variant_ == kFused)
       e = fast::forward(a, second, &cur_, plan, shot, store, it0, it1, zero, fin, stream());
@@ -940,7 +1012,7 @@ void Model::forward_simulate(int shot, bool store, bool verbose, bool output_wav
     run(n_steps, n_steps, false, true);
   }
   finish("forward_simulate");
-  if (!async_ && variant_ == kFusedTma) check_device_error();
+  if (!async_ && is_tma()) check_device_error();
   if (verbose) {
     synchronize();
     double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -962,6 +1034,22 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
   void *second[5] = {fields2_[0].get(), fields2_[1].get(), fields2_[2].get(), fields2_[3].get(),
                      fields2_[4].get()};
   cudaError_t err;
+  if (variant_ == kFusedTmaPersistent) {
+    // One launch for all steps: time it whole; the per-step figure is its
+    // share.
+    cudaEventRecord(ev.front(), stream());
+    err = tma_forward(shot, false, 0, n_steps, true, false, nullptr);
+    cudaEventRecord(ev.back(), stream());
+    cudaError_t sync = cudaStreamSynchronize(stream());
+    float ms = 0;
+    if (err == cudaSuccess && sync == cudaSuccess) cudaEventElapsedTime(&ms, ev.front(), ev.back());
+    for (auto &e : ev) cudaEventDestroy(e);
+    cuda_check(err, "profile_forward");
+    cuda_check(sync, "profile_forward");
+    if (per_step_ms) *per_step_ms = ms / n_steps;
+    if (kernel_ms && max_kernels > 0) kernel_ms[0] = ms / n_steps;
+    return 1;
+  }
   if (prec_ == PSV_FP64)
     err = forward_f64(a, plans_[shot], shot, false, 0, n_steps, true, false, stream());
   else if (variant_ == kFusedTma)
@@ -996,11 +1084,11 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
 }
 
 void Model::set_variant(int v) {
-  if (v != kFused && v != kTwoKernel && v != kFusedTma)
+  if (v != kFused && v != kTwoKernel && v != kFusedTma && v != kFusedTmaPersistent)
     throw Error(PSV_ERR_INVALID_ARGUMENT, "unknown kernel variant");
   if (prec_ == PSV_FP64 && v != kTwoKernel)
     throw Error(PSV_ERR_INVALID_ARGUMENT, "the fused variants are FP32 only");
-  if (v == kFusedTma && !tma_ok_)
+  if ((v == kFusedTma || v == kFusedTmaPersistent) && !tma_ok_)
     throw Error(PSV_ERR_INVALID_ARGUMENT, "the TMA variant needs driver tensor-map support");
   DeviceGuard guard(device_);
   if ((v == kTwoKernel) != (variant_ == kTwoKernel) && cur_ == 1) {
@@ -1019,6 +1107,7 @@ void Model::set_variant(int v) {
 const char *Model::step_kernel_name(int k) const {
   if (variant_ == kFused) return k == 0 ? "fused_step" : "";
   if (variant_ == kFusedTma) return k == 0 ? "fused_step_tma" : "";
+  if (variant_ == kFusedTmaPersistent) return k == 0 ? "fused_steps_tma" : "";
   return k == 0 ? "stress_step" : (k == 1 ? "velocity_step" : "");
 }
 
@@ -1035,7 +1124,7 @@ void Model::adjoint_simulate(int shot, bool verbose) {
     if (prec_ == PSV_FP64) {
       e = adjoint_f64(a, plans_[cfg_.n_shots], shot, stream());
       cur_ = 0;
-    } else if (variant_ == kFusedTma) {
+    } else if (is_tma()) {
       e = tma_adjoint(shot);
     } else if (variant_ == kFused) {
       e = fast::adjoint(a, second, &cur_, plans_[cfg_.n_shots], shot, stream());
@@ -1046,7 +1135,7 @@ void Model::adjoint_simulate(int shot, bool verbose) {
     cuda_check(e, "adjoint_simulate");
   });
   finish("adjoint_simulate");
-  if (!async_ && variant_ == kFusedTma) check_device_error();
+  if (!async_ && is_tma()) check_device_error();
   if (verbose) {
     synchronize();
     double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

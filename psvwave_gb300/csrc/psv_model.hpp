@@ -160,6 +160,7 @@ class Model {
   size_t exact_bytes(int checkpoint_every) const;
   int variant() const { return variant_; }
   int kernels_per_step() const { return variant_ == kTwoKernel ? 2 : 1; }
+  bool is_tma() const { return variant_ == kFusedTma || variant_ == kFusedTmaPersistent; }
   const char *step_kernel_name(int k) const;
 
   void set_stream(cudaStream_t s) { user_stream_ = s; }
@@ -245,6 +246,8 @@ class Model {
   DeviceBuffer rec_raw_;                      // [2][nr][nt]         (T)
   DeviceBuffer rec_cell_;                     // [nr] int
   DeviceBuffer rec_start_, rec_order_;        // receivers grouped by cell (exact adjoint)
+  DeviceBuffer rec_tile_start_, rec_tile_list_;  // receivers by tile (persistent step)
+  DeviceBuffer sched_;                        // persistent step: item counter, tile progress
   int n_rec_groups_ = 0;
   DeviceBuffer stf_d_;                        // [n_sources][nt]     (FP64)
   DeviceBuffer klame_[3];                     // lambda mu rho       (FP64)

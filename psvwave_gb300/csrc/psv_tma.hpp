@@ -44,6 +44,10 @@ struct alignas(128) SimDesc {
   float *rec_vx = nullptr, *rec_vz = nullptr;  // [nr][nt]
   InjPlan plan{};                 // forward: sources of the shot; adjoint: receivers
   const double *stf = nullptr, *a_ux = nullptr, *a_uz = nullptr;
+  // Receivers by tile of this descriptor's tile shape (tiles row-major over
+  // ceil(nz / TZ) tile columns): tile t holds receivers
+  // rec_list[rec_start[t] .. rec_start[t + 1]). Used by the persistent step.
+  const int *rec_start = nullptr, *rec_list = nullptr;
 };
 
 // True when tensor-map encoding is available and the row pitch is a
@@ -75,6 +79,24 @@ cudaError_t step(const SimDesc *sims, const int4 *tiles, int n_tiles, const int 
 // as a kernel parameter; tiles follow from the grid.
 cudaError_t step_single(const SimDesc &desc, int cfg, bool adjoint, int it, int parity,
                         bool store, int *err, cudaStream_t s);
+
+// n_steps time steps of one simulation in a single persistent launch: steps
+// it0, it0 + 1, ... (forward) or it0, it0 - 1, ... (adjoint), the first
+// reading set `parity0`. CTAs take (step, tile) items in step-major order
+// from a counter and start an item once the neighbouring tiles have
+// finished the previous step, so no step waits for the whole grid. `sched`
+// is device scratch of sched_words(...) zeroed words; errors (a timed-out
+// copy or dependency wait) raise *err.
+size_t sched_words(int cfg, int nx, int nz);
+cudaError_t steps_persistent(const SimDesc &desc, int cfg, bool adjoint, int it0, int n_steps,
+                             int parity0, bool store, int *err, unsigned *sched, cudaStream_t s);
+// Number of tiles of tile shape cfg over an nx x nz grid, and the tile of
+// point (ix, iz).
+int tile_count(int cfg, int nx, int nz);
+// CTAs of the persistent step of tile shape cfg that fit on the current
+// device at once (0 if the query fails).
+int resident_ctas(int cfg, bool adjoint);
+int tile_of(int cfg, int nz, int ix, int iz);
 
 }  // namespace tma
 }  // namespace psv

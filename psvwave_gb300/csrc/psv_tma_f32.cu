@@ -27,6 +27,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "psv_tma.hpp"
@@ -159,8 +160,9 @@ __device__ __forceinline__ bool interior_tile(const SimDesc &d, int X0, int Z0, 
 // the copies can be issued without waiting for any load) or from the
 // descriptor table (batch).
 template <class S, int CFG, bool ADJ>
-__device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, int X0, int Z0,
-                                          bool first, int it, int parity, int store, int *err) {
+__device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, int X0, int Z0,
+                                          bool first, int tile, int it, int parity, int store,
+                                          int *err, uint32_t phase, bool init_bar) {
   constexpr int TX = S::TX, TZ = S::TZ, W = S::W, VR = S::VR, SR = S::SR, G = S::G;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>(
@@ -181,11 +183,10 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
   const fast::Fields out = d.set[parity ^ 1];
   const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
 
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && init_bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(1)
                  : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   // Snapshot step: forward stores the pre-step state, adjoint correlates
   // with it (both at this shot's snapshot it / si).
@@ -211,6 +212,9 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
   griddep_wait();
   __syncthreads();
   if (threadIdx.x == 0) {
+    // Order this CTA's earlier generic accesses of the tile buffers before
+    // the copies overwrite them.
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                  "r"(S::TX_BYTES)
                  : "memory");
@@ -237,13 +241,25 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
 
   // Bounded wait (about a second at most); the CTA agrees on the outcome so
   // that it leaves together, after its copies have landed.
-  const bool landed = mbar_wait(bar, 0, 1u << 20);
+  const bool landed = mbar_wait(bar, phase, 1u << 20);
   if (__syncthreads_or(!landed)) {
     if (threadIdx.x == 0) {
       atomicOr(err, 1);
-      mbar_wait(bar, 0, 1u << 20);
+      mbar_wait(bar, phase, 1u << 20);
     }
-    return;
+    return false;
+  }
+  // Persistent step: the tile records its own receivers (pre-step
+  // velocities) from the copied tile.
+  if (!ADJ && tile >= 0 && d.rec_start) {
+    const int r1 = d.rec_start[tile + 1];
+    for (int i = d.rec_start[tile] + threadIdx.x; i < r1; i += S::NT) {
+      const int r = d.rec_list[i];
+      const int c = d.rec_cell[r];
+      const int ix = c / ps, iz = c - ix * ps;
+      d.rec_vx[(size_t)r * d.nt + it] = sv[0][ix - X0 + 4][iz - Z0 + 4];
+      d.rec_vz[(size_t)r * d.nt + it] = sv1[ix - X0 + 4][iz - Z0 + 4];
+    }
   }
 
   const float dtv = ADJ ? -d.dt : d.dt;
@@ -332,7 +348,7 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
         }
       }
     }
-    return;
+    return true;
   }
 
   const int np = d.np;
@@ -433,6 +449,7 @@ __device__ __forceinline__ void step_body(const SimDesc &d, const Maps &maps, in
       out.vz[gp] = vz;
     }
   }
+  return true;
 }
 
 // Single simulation: tensor maps as a parameter, tiles from blockIdx
@@ -442,8 +459,8 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
     fused_step_tma(const __grid_constant__ SimDesc d, int tiles_z, int it, int parity, int store,
                    int *err) {
   const int bx = blockIdx.x, tx = bx / tiles_z, tz = bx - tx * tiles_z;
-  step_body<S, CFG, ADJ>(d, d.maps[parity], tx * S::TX, tz * S::TZ, bx == 0, it, parity, store,
-                         err);
+  step_body<S, CFG, ADJ>(d, d.maps[parity], tx * S::TX, tz * S::TZ, bx == 0, -1, it, parity,
+                         store, err, 0u, true);
 }
 
 // Many simulations: tile table entries (sim, x0, z0, first) per CTA. With
@@ -455,7 +472,86 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
   const int4 t = tiles[blockIdx.x];
   if (active && !active[t.x]) return;
   const SimDesc &d = sims[t.x];
-  step_body<S, CFG, ADJ>(d, d.maps[parity], t.y, t.z, t.w != 0, it, parity, store, err);
+  step_body<S, CFG, ADJ>(d, d.maps[parity], t.y, t.z, t.w != 0, -1, it, parity, store, err, 0u,
+                         true);
+}
+
+// Bounded wait until the counter at p reaches v (acquire): true when it did.
+// After 64 plain polls each round sleeps about 100 ns; 2^22 rounds bound
+// the wait to a few seconds at most.
+__device__ __forceinline__ bool wait_at_least(const unsigned *p, unsigned v) {
+  for (uint32_t i = 0; i < (1u << 22); ++i) {
+    unsigned x;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(x) : "l"(p) : "memory");
+    if (x >= v) return true;
+    if (i >= 64) __nanosleep(100);  // poll first: most waits are short
+  }
+  return false;
+}
+
+// All time steps of one simulation in one launch. sched[0] hands out items
+// w = step * n_tiles + tile in increasing order (a CTA holds at most its
+// current item and the next); sched[1 + t] counts the steps tile t has
+// finished. An item starts once the tile and its eight
+// neighbours have finished the previous step: that is everything the step
+// reads (halos are at most 4 points, less than a tile), and it also
+// guarantees that no neighbour still reads the buffer the step overwrites.
+// The earliest unfinished item always has its inputs ready, so the
+// schedule cannot deadlock; each wait is bounded nonetheless, and a CTA
+// that gives up raises *err and stops (its dependents then time out too).
+template <class S, int CFG, bool ADJ>
+__global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
+    fused_steps_tma(const __grid_constant__ SimDesc d, int tiles_x, int tiles_z, int it0,
+                    int n_steps, int parity0, int store, int *err, unsigned *sched) {
+  __shared__ int s_item;
+  const int n_tiles = tiles_x * tiles_z;
+  const long long total = (long long)n_steps * n_tiles;
+  uint32_t phase = 0;
+  bool init = true;
+  // Thread 0 fetches the next item while the current one runs.
+  unsigned next = 0;
+  if (threadIdx.x == 0) next = atomicAdd(sched, 1u);
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = (int)next;
+      next = atomicAdd(sched, 1u);
+    }
+    __syncthreads();
+    const long long w = s_item;
+    if (w >= total) return;
+    const int j = (int)(w / n_tiles), tile = (int)(w - (long long)j * n_tiles);
+    const int tx = tile / tiles_z, tz = tile - tx * tiles_z;
+    if (j > 0) {
+      // Nine threads wait on the tile and its eight neighbours at once.
+      bool ok = true;
+      if (threadIdx.x < 9) {
+        const int a = tx + (int)threadIdx.x / 3 - 1, b = tz + (int)threadIdx.x % 3 - 1;
+        if (a >= 0 && a < tiles_x && b >= 0 && b < tiles_z)
+          ok = wait_at_least(sched + 1 + a * tiles_z + b, (unsigned)j);
+      }
+      if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0) atomicOr(err, 2);
+        return;
+      }
+      // The copies (async proxy) must see what the generic stores of other
+      // CTAs made visible to the waiting threads.
+      if (threadIdx.x == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
+    const int it = ADJ ? it0 - j : it0 + j;
+    const int parity = parity0 ^ (j & 1);
+    if (!step_body<S, CFG, ADJ>(d, d.maps[parity], tx * S::TX, tz * S::TZ, false, tile, it, parity,
+                                store, err, phase, init))
+      return;
+    phase ^= 1u;
+    init = false;
+    __syncthreads();  // every thread's stores of the item are issued
+    if (threadIdx.x == 0) {
+      __threadfence();
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + tile),
+                   "r"((unsigned)(j + 1))
+                   : "memory");
+    }
+  }
 }
 
 // The shared-memory opt-in is a per-device attribute: set it once per device.
@@ -483,6 +579,43 @@ cudaError_t launch(const SimDesc *sims, const int4 *tiles, int n_tiles, const in
   fused_step_tma_batch<S, CFG, ADJ><<<n_tiles, S::NT, S::SMEM, s>>>(sims, tiles, active, it,
                                                                     parity, store, err);
   return cudaGetLastError();
+}
+
+template <class S, int CFG, bool ADJ>
+cudaError_t launch_persistent(const SimDesc &d, int it0, int n_steps, int parity0, int store,
+                              int *err, unsigned *sched, cudaStream_t s) {
+  static unsigned long long configured = 0;
+  cudaError_t e = configure(fused_steps_tma<S, CFG, ADJ>, S::SMEM, configured);
+  if (e != cudaSuccess) return e;
+  if (n_steps <= 0) return cudaSuccess;
+  const int tiles_x = (d.nx + S::TX - 1) / S::TX, tiles_z = (d.nz + S::TZ - 1) / S::TZ;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_steps_tma<S, CFG, ADJ>,
+                                                         S::NT, S::SMEM)) != cudaSuccess)
+    return e;
+  const long long items = (long long)n_steps * tiles_x * tiles_z;
+  // At most the resident CTAs, and at most two steps' worth of tiles: more
+  // CTAs would only hold items further ahead and poll for them.
+  const long long slots = (long long)std::max(per_sm, 1) * sms;
+  const int grid = (int)std::min(std::min<long long>(items, slots), 2LL * tiles_x * tiles_z);
+  if (items + grid >= 0x7fffffffLL) return cudaErrorInvalidValue;  // item numbers are 31-bit
+  // Cooperative launch: every CTA is resident at once, as CTAs that wait on
+  // one another require.
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(grid);
+  lc.blockDim = dim3(S::NT);
+  lc.dynamicSmemBytes = S::SMEM;
+  lc.stream = s;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, fused_steps_tma<S, CFG, ADJ>, d, tiles_x, tiles_z, it0, n_steps,
+                            parity0, store, err, sched);
 }
 
 template <class S, int CFG, bool ADJ>
@@ -597,6 +730,55 @@ cudaError_t step_single(const SimDesc &d, int cfg, bool adjoint, int it, int par
                    : launch_single<Small, kTile16x28, false>(d, it, parity, st, err, s);
   return adjoint ? launch_single<Big, kTile32x60, true>(d, it, parity, st, err, s)
                  : launch_single<Big, kTile32x60, false>(d, it, parity, st, err, s);
+}
+
+int tile_count(int cfg, int nx, int nz) {
+  int tx, tz;
+  tile_dims(cfg, &tx, &tz);
+  return ((nx + tx - 1) / tx) * ((nz + tz - 1) / tz);
+}
+
+int tile_of(int cfg, int nz, int ix, int iz) {
+  int tx, tz;
+  tile_dims(cfg, &tx, &tz);
+  return (ix / tx) * ((nz + tz - 1) / tz) + iz / tz;
+}
+
+size_t sched_words(int cfg, int nx, int nz) { return 1 + (size_t)tile_count(cfg, nx, nz); }
+
+namespace {
+template <class S, int CFG, bool ADJ>
+int resident() {
+  static unsigned long long configured = 0;
+  if (configure(fused_steps_tma<S, CFG, ADJ>, S::SMEM, configured) != cudaSuccess) return 0;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_steps_tma<S, CFG, ADJ>, S::NT,
+                                                    S::SMEM) != cudaSuccess)
+    return 0;
+  return per_sm * sms;
+}
+}  // namespace
+
+int resident_ctas(int cfg, bool adjoint) {
+  if (cfg == kTile16x28)
+    return adjoint ? resident<Small, kTile16x28, true>() : resident<Small, kTile16x28, false>();
+  return adjoint ? resident<Big, kTile32x60, true>() : resident<Big, kTile32x60, false>();
+}
+
+cudaError_t steps_persistent(const SimDesc &d, int cfg, bool adjoint, int it0, int n_steps,
+                             int parity0, bool store, int *err, unsigned *sched, cudaStream_t s) {
+  const int st = store ? 1 : 0;
+  if (cfg == kTile16x28)
+    return adjoint ? launch_persistent<Small, kTile16x28, true>(d, it0, n_steps, parity0, st, err,
+                                                                sched, s)
+                   : launch_persistent<Small, kTile16x28, false>(d, it0, n_steps, parity0, st,
+                                                                 err, sched, s);
+  return adjoint ? launch_persistent<Big, kTile32x60, true>(d, it0, n_steps, parity0, st, err,
+                                                            sched, s)
+                 : launch_persistent<Big, kTile32x60, false>(d, it0, n_steps, parity0, st, err,
+                                                             sched, s);
 }
 
 cudaError_t step(const SimDesc *sims, const int4 *tiles, int n_tiles, const int *active, int cfg,

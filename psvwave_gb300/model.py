@@ -493,16 +493,17 @@ class fdModel:
         names = [self._lib.psv_step_kernel_name(self._h, k).decode() for k in range(n.value)]
         return per_step.value, dict(zip(names, list(ks)[:n.value]))
 
-    VARIANTS = {"fused": 0, "two_kernel": 1, "fused_tma": 2}
+    VARIANTS = {"fused": 0, "two_kernel": 1, "fused_tma": 2, "fused_tma_persistent": 3}
 
     @property
     def kernel_variant(self):
         """'fused_tma' (one launch per step with TMA tile loads; the FP32
-        default), 'fused' (one launch per step, FP32) or
+        default), 'fused_tma_persistent' (the same step, all time steps in
+        one persistent launch), 'fused' (one launch per step, FP32) or
         'two_kernel' (stress and velocity launches; the FP64 variant)."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_get_kernel_variant(self._h, ctypes.byref(v)))
-        return {0: "fused", 1: "two_kernel", 2: "fused_tma"}[v.value]
+        return {0: "fused", 1: "two_kernel", 2: "fused_tma", 3: "fused_tma_persistent"}[v.value]
 
     @kernel_variant.setter
     def kernel_variant(self, name):
@@ -522,7 +523,9 @@ class fdModel:
         _capi.check(self._lib.psv_set_tile_shape(self._h, self.TILE_SHAPES[name]))
 
     def autotune(self, n_steps=50):
-        """Time every tile shape on n_steps forward steps; keep the fastest."""
+        """Time every tile shape with both TMA launch schemes (one launch per
+        step, one persistent launch) on n_steps forward steps; keep the
+        fastest pair and return its tile shape."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_autotune(self._h, int(n_steps), ctypes.byref(v)))
         return {0: "32x60", 1: "16x28"}[v.value]

@@ -232,3 +232,15 @@ def test_graph_replay_matches_eager(golden, precision):
         res.append((m.get_synthetic_data()[0], m.get_kernels()[1], m.get_wavefields()[0]))
     for a, b in zip(res[0], res[1]):
         assert np.array_equal(a, b)
+
+
+def test_large_grid_defaults_to_persistent_launch():
+    # 2100 x 900 points: 990 tiles of 32 x 60 per step, at least a full wave
+    # of resident CTAs, so every time step runs in one persistent launch.
+    from psvwave_gb300 import workloads
+
+    m = psv.fdModel.from_parameters(workloads.c1_params(nt=10))
+    assert m.tile_shape == "32x60"
+    assert m.kernel_variant == "fused_tma_persistent"
+    small = psv.fdModel(SMALL_INI)
+    assert small.kernel_variant == "fused_tma"

@@ -165,7 +165,7 @@ def test_default_variants():
         psv.fdModel(SMALL_INI, precision="fp64").kernel_variant = "fused_tma"
 
 
-@pytest.mark.parametrize("variant", ["fused_tma", "fused", "two_kernel"])
+@pytest.mark.parametrize("variant", ["fused_tma", "fused_tma_persistent", "fused", "two_kernel"])
 def test_fp32_variants_within_tolerance(golden, variant):
     m = psv.fdModel(SMALL_INI, precision="fp32")
     m.kernel_variant = variant
@@ -236,3 +236,38 @@ def test_tile_shapes_agree_and_autotune(golden):
         assert rel_l2(res["32x60"][name], res["16x28"][name]) <= 1e-5
     m = psv.fdModel(SMALL_INI, precision="fp32")
     assert m.autotune(20) in ("32x60", "16x28")
+
+
+@pytest.mark.parametrize("shape", ["32x60", "16x28"])
+@pytest.mark.parametrize("ini", [SMALL_INI, NB2_INI])
+def test_persistent_step_matches_per_step_launches_bitwise(golden, shape, ini):
+    """The persistent variant runs the per-step variant's arithmetic tile by
+    tile, only scheduled differently (a tile starts a step once its
+    neighbours have finished the previous one): forward seismograms and
+    snapshots, and the adjoint's kernels, are identical bit for bit."""
+    res = []
+    for variant in ("fused_tma", "fused_tma_persistent"):
+        m = psv.fdModel(ini, precision="fp32")
+        m.kernel_variant = variant
+        m.tile_shape = shape
+        if ini == SMALL_INI:
+            target, start = tuple(golden["target"]), tuple(golden["start"])
+        else:
+            target, start = nb2_media(m.nx, m.nz, m.np_boundary, m.dx, m.dz)
+        m.set_parameter_fields(*target)
+        for s in range(m.n_shots):
+            m.forward_simulate(s, False)
+        m.set_observed_data(*m.get_synthetic_data())
+        m.set_parameter_fields(*start)
+        for s in range(m.n_shots):
+            m.forward_simulate(s, True)
+        m.calculate_l2_misfit()
+        m.calculate_l2_adjoint_sources()
+        m.reset_kernels()
+        for s in range(m.n_shots):
+            m.adjoint_simulate(s)
+        res.append((m.get_synthetic_data(), m.get_snapshots(), m.get_lame_kernels(), m.misfit))
+    (d0, s0, k0, m0), (d1, s1, k1, m1) = res
+    assert m0 == m1
+    for a, b in zip(d0 + s0 + k0, d1 + s1 + k1):
+        assert np.array_equal(a, b)
