@@ -55,6 +55,8 @@ struct AdjArgs {
   const T *ftxx, *ftzz, *ftxz;
   // FP64 medium gradients, unpadded [nx][nz]
   double *g_lm, *g_la, *g_mu, *g_b;
+  // scratch, padded: w = b dt T lv (step 1) and p_x, p_z, q = dt C y (step 2)
+  T *wx, *wz, *px, *pz, *qq;
 };
 
 template <typename T>
@@ -76,6 +78,42 @@ __device__ __forceinline__ T w_at(const AdjArgs<T> &a, const T *lv, int ix, int 
   return a.b[p] * a.dt * taper_of(a, ix, iz) * lv[p];
 }
 
+// A padded scratch field at (x, z), 0 outside the grid (the fields hold 0
+// outside the interior already).
+template <typename T>
+__device__ __forceinline__ T at(const AdjArgs<T> &a, const T *f, int x, int z) {
+  if (x < 0 || x >= a.nx || z < 0 || z >= a.nz) return T(0);
+  return f[(size_t)x * a.pitch + z];
+}
+
+// w = b dt T lv, once per point (each is used at 9 stencil points).
+template <typename T>
+__global__ void w_fields(AdjArgs<T> a) {
+  const int iz = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ix = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= a.nx || iz >= a.nz) return;
+  const size_t p = (size_t)ix * a.pitch + iz;
+  a.wx[p] = w_at(a, a.lvx, ix, iz);
+  a.wz[p] = w_at(a, a.lvz, ix, iz);
+}
+
+// p_x, p_z, q = dt C y of the updated adjoint stresses, once per point.
+template <typename T>
+__device__ __forceinline__ void pq_at(const AdjArgs<T> &a, int ix, int iz, T &px, T &pz, T &q);
+
+template <typename T>
+__global__ void pq_fields(AdjArgs<T> a) {
+  const int iz = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ix = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= a.nx || iz >= a.nz) return;
+  const size_t p = (size_t)ix * a.pitch + iz;
+  T px, pz, q;
+  pq_at(a, ix, iz, px, pz, q);
+  a.px[p] = px;
+  a.pz[p] = pz;
+  a.qq[p] = q;
+}
+
 template <typename T>
 __global__ void velocity_transpose(AdjArgs<T> a, InjPlan plan, const double *stf, int nt,
                                    int it, double dt_d) {
@@ -86,8 +124,8 @@ __global__ void velocity_transpose(AdjArgs<T> a, InjPlan plan, const double *stf
   const size_t p = (size_t)ix * a.pitch + iz;
   const size_t u = (size_t)ix * a.nz + iz;
   // A^T w with A^T = (-Dx+ on txx, -Dz- and -Dx- ... ) as in the header.
-  auto wx = [&](int x, int z) { return w_at(a, a.lvx, x, z); };
-  auto wz = [&](int x, int z) { return w_at(a, a.lvz, x, z); };
+  auto wx = [&](int x, int z) { return at(a, a.wx, x, z); };
+  auto wz = [&](int x, int z) { return at(a, a.wz, x, z); };
   // -D+_x(wx)(j) / dx into txx: D+ g(j) = c1 (g(j+1) - g(j)) + c2 (g(j-1) - g(j+2))
   const T dxp_wx = c1 * (wx(ix + 1, iz) - wx(ix, iz)) + c2 * (wx(ix - 1, iz) - wx(ix + 2, iz));
   const T dzp_wx = c1 * (wx(ix, iz + 1) - wx(ix, iz)) + c2 * (wx(ix, iz - 1) - wx(ix, iz + 2));
@@ -164,21 +202,15 @@ __global__ void stress_transpose(AdjArgs<T> a) {
   a.otxz[p] = tp * a.ltxz[p];
   // E^T (dt C y):  v-bar_x += -D-_x(p_x)/dx - D-_z(q)/dz,
   //                v-bar_z += -D+_z(p_z)/dz - D+_x(q)/dx
-  T px0, pz0, q0, t0, t1, t2;
-  pq_at(a, ix, iz, px0, pz0, q0);
-  T pxm1, pxm2, pxp1, qzm1, qzm2, qzp1, pzp1, pzp2, pzm1, qxp1, qxp2, qxm1;
-  pq_at(a, ix - 1, iz, pxm1, t1, t2);
-  pq_at(a, ix - 2, iz, pxm2, t1, t2);
-  pq_at(a, ix + 1, iz, pxp1, t1, t2);
-  pq_at(a, ix, iz - 1, t0, t1, qzm1);
-  pq_at(a, ix, iz - 2, t0, t1, qzm2);
-  pq_at(a, ix, iz + 1, t0, t1, qzp1);
-  pq_at(a, ix, iz + 1, t0, pzp1, t2);
-  pq_at(a, ix, iz + 2, t0, pzp2, t2);
-  pq_at(a, ix, iz - 1, t0, pzm1, t2);
-  pq_at(a, ix + 1, iz, t0, t1, qxp1);
-  pq_at(a, ix + 2, iz, t0, t1, qxp2);
-  pq_at(a, ix - 1, iz, t0, t1, qxm1);
+  const T px0 = at(a, a.px, ix, iz), pz0 = at(a, a.pz, ix, iz), q0 = at(a, a.qq, ix, iz);
+  const T pxm1 = at(a, a.px, ix - 1, iz), pxm2 = at(a, a.px, ix - 2, iz),
+          pxp1 = at(a, a.px, ix + 1, iz);
+  const T qzm1 = at(a, a.qq, ix, iz - 1), qzm2 = at(a, a.qq, ix, iz - 2),
+          qzp1 = at(a, a.qq, ix, iz + 1);
+  const T pzp1 = at(a, a.pz, ix, iz + 1), pzp2 = at(a, a.pz, ix, iz + 2),
+          pzm1 = at(a, a.pz, ix, iz - 1);
+  const T qxp1 = at(a, a.qq, ix + 1, iz), qxp2 = at(a, a.qq, ix + 2, iz),
+          qxm1 = at(a, a.qq, ix - 1, iz);
   const T dxm_px = c1 * (px0 - pxm1) + c2 * (pxm2 - pxp1);
   const T dzm_q = c1 * (q0 - qzm1) + c2 * (qzm2 - qzp1);
   const T dzp_pz = c1 * (pzp1 - pz0) + c2 * (pzm1 - pzp2);
@@ -258,8 +290,15 @@ __global__ void add_receiver_terms(int n_groups, int nt, int it, const int *cell
     a.g_la = e.g_la;                                                                          \
     a.g_mu = e.g_mu;                                                                          \
     a.g_b = e.g_b;                                                                            \
+    a.wx = (T *)e.scratch[0];                                                                 \
+    a.wz = (T *)e.scratch[1];                                                                 \
+    a.px = (T *)e.scratch[2];                                                                 \
+    a.pz = (T *)e.scratch[3];                                                                 \
+    a.qq = (T *)e.scratch[4];                                                                 \
     const dim3 block(32, 8), grid((e.nz + 31) / 32, (e.nx + 7) / 8);                          \
+    exact::w_fields<T><<<grid, block, 0, s>>>(a);                                             \
     exact::velocity_transpose<T><<<grid, block, 0, s>>>(a, e.plan, e.stf, e.nt, e.it, e.dt);  \
+    exact::pq_fields<T><<<grid, block, 0, s>>>(a);                                            \
     exact::stress_transpose<T><<<grid, block, 0, s>>>(a);                                     \
     if (e.n_rec_groups)                                                                       \
       exact::add_receiver_terms<T><<<(2 * e.n_rec_groups + 127) / 128, 128, 0, s>>>(         \

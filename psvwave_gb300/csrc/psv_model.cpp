@@ -509,7 +509,7 @@ size_t Model::exact_bytes(int C) const {
   if (C <= 0 || C > nt) C = nt;
   const size_t state = 5 * padded_size() * elem();
   const size_t n_ck = (nt + C - 1) / C;
-  return n_ck * state + (C + 1) * state + 8 * padded_size() * elem() +
+  return n_ck * state + (C + 1) * state + 13 * padded_size() * elem() +
          7 * grid_size() * sizeof(double);
 }
 
@@ -548,6 +548,7 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
   for (auto &b : kexact_) ensure(b, g * sizeof(double));
   for (auto &b : adj_) ensure(b, data_size() * sizeof(double));
   for (auto &b : lam_) ensure(b, gp * e);
+  for (auto &b : exs_) ensure(b, gp * e);
   ensure(ckpt_, n_ck * state_bytes);
   ensure(slots_, (C + 1) * state_bytes);
   if (grown) clear_graphs();
@@ -717,6 +718,7 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
         x.n_rec_groups = n_rec_groups_;
         x.rec_start = rec_start_.as<int>();
         x.rec_order = rec_order_.as<int>();
+        for (int f = 0; f < 5; ++f) x.scratch[f] = exs_[f].get();
         x.adj_x = adj_[0].as<double>() + off;
         x.adj_z = adj_[1].as<double>() + off;
         cuda_check(prec_ == PSV_FP64 ? exact_step_f64(x, s) : exact_step_f32(x, s), "exact step");

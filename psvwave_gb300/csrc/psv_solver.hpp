@@ -116,6 +116,7 @@ struct ExactStepArgs {
   int n_rec_groups = 0;
   const int *rec_start = nullptr, *rec_order = nullptr;
   const double *adj_x = nullptr, *adj_z = nullptr;  // receiver terms [nr][nt] of the shot
+  void *scratch[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // padded grids
 };
 cudaError_t exact_step_f32(const ExactStepArgs &e, cudaStream_t s);
 cudaError_t exact_step_f64(const ExactStepArgs &e, cudaStream_t s);
