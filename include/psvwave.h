@@ -306,6 +306,12 @@ int psv_batch_info(const psv_batch *b, int *members, int *tiles, double *cells);
  * flags[k] != 0; NULL = all (the default). Inactive members' CTAs exit at
  * once, so the captured time loop serves every subset. */
 int psv_batch_set_active(psv_batch *b, const int *flags, int n);
+/* Launch scheme of psv_batch_forward: 0 (the default) launches once per
+ * time step, the loop captured as one CUDA graph; persistent != 0 runs every
+ * time step of every member in one persistent launch over the batch's tile
+ * table, tiles starting a step as soon as their neighbours have finished the
+ * previous one. Results are identical. */
+int psv_batch_set_persistent(psv_batch *b, int persistent);
 
 /* ---- no-allocation entry point ------------------------------------------ */
 /* L2 misfit 0.5 dt sum((obs - syn)^2) over both components, written to the

@@ -38,6 +38,18 @@ class Batch:
         for s in range(model.n_shots):
             self.add(model, s)
 
+    @property
+    def persistent(self):
+        return getattr(self, "_persistent", False)
+
+    @persistent.setter
+    def persistent(self, on):
+        """Launch scheme: one launch per time step, captured as one graph
+        (False, the default), or every step in one persistent launch (True).
+        Results are identical."""
+        _capi.check(self._lib.psv_batch_set_persistent(self._h, int(bool(on))))
+        self._persistent = bool(on)
+
     def set_active(self, mask=None):
         """Members the next forward() advances (a boolean per member, in the
         order added); None = all."""

@@ -74,6 +74,8 @@ void Batch::build() {
   raw_.allocate(std::max<size_t>(raw, 1) * sizeof(float));
   std::vector<tma::SimDesc> descs(members_.size());
   std::vector<int4> tiles[tma::kNumTileCfgs];
+  std::vector<int> rec_start, rec_list;  // per member: tiles + 1 offsets; receivers
+  std::vector<size_t> rec_start_off(members_.size());
   float *next = arena_.as<float>();
   for (size_t k = 0; k < members_.size(); ++k) {
     Model &m = *members_[k].first;
@@ -112,9 +114,43 @@ void Batch::build() {
     d.stf = m.stf_d_.as<double>();
     if (!tma::make_maps(d, m.mu_.as<float>(), tile_cfg_))
       throw Error(PSV_ERR_CUDA, "tensor-map encoding failed for a batch member");
+    int tx, tz;
+    tma::tile_dims(tile_cfg_, &tx, &tz);
+    d.tile_base = static_cast<int>(tiles[tile_cfg_].size());
+    d.tiles_x = (g.nx + tx - 1) / tx;
+    d.tiles_z = (g.nz + tz - 1) / tz;
     for (int cfg = 0; cfg < tma::kNumTileCfgs; ++cfg)
       tma::append_tiles(cfg, static_cast<int>(k), g.nx, g.nz, tiles[cfg]);
+    // This member's receivers by tile, for the persistent scheme.
+    const int nt_m = d.tiles_x * d.tiles_z;
+    const size_t s0 = rec_start.size(), l0 = rec_list.size();
+    rec_start_off[k] = s0;
+    rec_start.resize(s0 + nt_m + 1, 0);
+    for (int r = 0; r < c.nr; ++r)
+      ++rec_start[s0 + 1 + tma::tile_of(tile_cfg_, g.nz, m.ix_rec_[r], m.iz_rec_[r])];
+    for (int t = 0; t < nt_m; ++t) rec_start[s0 + t + 1] += rec_start[s0 + t];
+    for (int t = 0; t <= nt_m; ++t) rec_start[s0 + t] += static_cast<int>(l0);
+    rec_list.resize(l0 + c.nr);
+    std::vector<int> fill(rec_start.begin() + s0, rec_start.begin() + s0 + nt_m);
+    for (int r = 0; r < c.nr; ++r)
+      rec_list[fill[tma::tile_of(tile_cfg_, g.nz, m.ix_rec_[r], m.iz_rec_[r])]++] = r;
   }
+  rec_start_.allocate(std::max<size_t>(rec_start.size(), 1) * sizeof(int));
+  rec_list_.allocate(std::max<size_t>(rec_list.size(), 1) * sizeof(int));
+  if (!rec_start.empty())
+    cuda_check(cudaMemcpy(rec_start_.get(), rec_start.data(), rec_start.size() * sizeof(int),
+                          cudaMemcpyHostToDevice),
+               "upload batch receiver tiles");
+  if (!rec_list.empty())
+    cuda_check(cudaMemcpy(rec_list_.get(), rec_list.data(), rec_list.size() * sizeof(int),
+                          cudaMemcpyHostToDevice),
+               "upload batch receiver tiles");
+  for (size_t k = 0; k < members_.size(); ++k) {
+    descs[k].rec_start = rec_start_.as<int>() + rec_start_off[k];
+    descs[k].rec_list = rec_list_.as<int>();
+  }
+  sched_.allocate(tma::sched_words_batch(static_cast<int>(tiles[tile_cfg_].size())) *
+                  sizeof(unsigned));
   active_.allocate(members_.size() * sizeof(int));
   descs_d_.allocate(descs.size() * sizeof(tma::SimDesc));
   cuda_check(cudaMemcpy(descs_d_.get(), descs.data(), descs.size() * sizeof(tma::SimDesc),
@@ -136,6 +172,12 @@ void Batch::set_tile_cfg(int cfg) {
   clear_graphs();
   tile_cfg_ = cfg;
   built_ = false;  // the descriptors' tensor maps depend on the tile shape
+}
+
+void Batch::set_persistent(bool on) {
+  if (on == persistent_) return;
+  persistent_ = on;
+  clear_graphs();
 }
 
 void Batch::set_active(const int *flags, int n) {
@@ -177,13 +219,22 @@ void Batch::forward(bool store, int n_steps) {
   const int cfg = tile_cfg_;
   auto enqueue = [&]() {
     cuda_check(cudaMemsetAsync(arena_.get(), 0, arena_.bytes(), stream_), "batch zero");
-    int parity = 0;
-    for (int it = 0; it < steps; ++it) {
-      cuda_check(tma::step(descs_d_.as<tma::SimDesc>(), tiles_d_[cfg].as<int4>(), n_tiles_[cfg],
-                           active_.as<int>(), cfg, false, it, parity, store,
-                           err_flag_.as<int>(), stream_),
-                 "batch step");
-      parity ^= 1;
+    if (persistent_) {
+      cuda_check(cudaMemsetAsync(sched_.get(), 0, sched_.bytes(), stream_), "batch schedule");
+      cuda_check(tma::steps_persistent_batch(descs_d_.as<tma::SimDesc>(),
+                                             tiles_d_[cfg].as<int4>(), n_tiles_[cfg],
+                                             active_.as<int>(), cfg, steps, store,
+                                             err_flag_.as<int>(), sched_.as<unsigned>(), stream_),
+                 "batch steps");
+    } else {
+      int parity = 0;
+      for (int it = 0; it < steps; ++it) {
+        cuda_check(tma::step(descs_d_.as<tma::SimDesc>(), tiles_d_[cfg].as<int4>(),
+                             n_tiles_[cfg], active_.as<int>(), cfg, false, it, parity, store,
+                             err_flag_.as<int>(), stream_),
+                   "batch step");
+        parity ^= 1;
+      }
     }
     for (size_t k = 0; k < members_.size(); ++k) {
       Model &m = *members_[k].first;
@@ -194,7 +245,7 @@ void Batch::forward(bool store, int n_steps) {
       cuda_check(receiver_cumsum_f32(c.nr, c.nt, steps, c.dt, c.dx * c.dz, raw,
                                      raw + static_cast<size_t>(c.nr) * nt_,
                                      m.rtf_[0].as<double>() + off, m.rtf_[1].as<double>() + off,
-                                     stream_),
+                                     stream_, active_.as<int>(), static_cast<int>(k)),
                  "batch seismograms");
     }
   };

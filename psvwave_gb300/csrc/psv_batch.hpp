@@ -35,6 +35,12 @@ class Batch {
   // Which members the next forward() advances (non-zero = advance); all of
   // them by default. The others keep their previous seismograms.
   void set_active(const int *flags, int n);
+  // Launch scheme: one launch per time step (false, the default) or every
+  // step in one persistent launch over the tile table (true). A batch step
+  // holds tens of thousands of tiles, many waves with no tail to recover,
+  // so the per-item scheduling of the persistent scheme is measured slower.
+  void set_persistent(bool on);
+  bool persistent() const { return persistent_; }
   int tile_cfg() const { return tile_cfg_; }
   int size() const { return static_cast<int>(members_.size()); }
   double cells() const;  // grid points summed over members
@@ -59,6 +65,9 @@ class Batch {
   DeviceBuffer err_flag_;
   DeviceBuffer active_;              // per member flag, read by the step kernel
   std::vector<int> active_h_;
+  bool persistent_ = false;
+  DeviceBuffer sched_;               // persistent scheme: item counter, tile progress
+  DeviceBuffer rec_start_, rec_list_;  // receivers by member tile (persistent scheme)
   std::vector<size_t> raw_off_;  // per member, floats into raw_
   struct Graph {
     cudaGraphExec_t exec = nullptr;

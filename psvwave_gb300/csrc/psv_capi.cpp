@@ -617,6 +617,13 @@ int psv_batch_autotune(psv_batch *b, int n_steps, int *chosen) {
   });
 }
 
+int psv_batch_set_persistent(psv_batch *b, int persistent) {
+  return guarded([&] {
+    need(b, "batch");
+    b->impl.set_persistent(persistent != 0);
+  });
+}
+
 int psv_batch_set_active(psv_batch *b, const int *flags, int n) {
   return guarded([&] {
     need(b, "batch");

@@ -122,9 +122,12 @@ cudaError_t exact_step_f32(const ExactStepArgs &e, cudaStream_t s);
 cudaError_t exact_step_f64(const ExactStepArgs &e, cudaStream_t s);
 
 // Seismograms from raw FP32 receiver velocities (psv_solver_f32.cu).
+// With `active` non-null, nothing is written unless active[member] != 0
+// (batched runs whose member set varies between replays of one graph).
 cudaError_t receiver_cumsum_f32(int nr, int nt, int n_steps, double dt, double dxdz,
                                 const float *raw_x, const float *raw_z, double *out_x,
-                                double *out_z, cudaStream_t s);
+                                double *out_z, cudaStream_t s, const int *active = nullptr,
+                                int member = 0);
 
 // FP64 helpers (psv_aux.cu).
 cudaError_t misfit_l2(size_t n, double dt, const double *obs_ux, const double *syn_ux,

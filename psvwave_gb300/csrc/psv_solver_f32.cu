@@ -17,10 +17,11 @@ namespace kern {
 __global__ void __launch_bounds__(256) receiver_scan(int nr, int nt, int n_steps, double dt,
                                                      double dxdz, const float *raw_x,
                                                      const float *raw_z, double *rtf_x,
-                                                     double *rtf_z) {
+                                                     double *rtf_z, const int *active,
+                                                     int member) {
   __shared__ double warp_total[8];
   const int k = blockIdx.x;
-  if (k >= 2 * nr) return;
+  if (k >= 2 * nr || (active && !active[member])) return;
   const int r = k >> 1, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float *raw = ((k & 1) ? raw_z : raw_x) + (size_t)r * nt;
   double *out = ((k & 1) ? rtf_z : rtf_x) + (size_t)r * nt;
@@ -52,10 +53,10 @@ __global__ void __launch_bounds__(256) receiver_scan(int nr, int nt, int n_steps
 
 cudaError_t receiver_cumsum_f32(int nr, int nt, int n_steps, double dt, double dxdz,
                                 const float *raw_x, const float *raw_z, double *out_x,
-                                double *out_z, cudaStream_t s) {
+                                double *out_z, cudaStream_t s, const int *active, int member) {
   if (nr <= 0) return cudaSuccess;
   kern::receiver_scan<<<2 * nr, 256, 0, s>>>(nr, nt, n_steps, dt, dxdz, raw_x, raw_z, out_x,
-                                              out_z);
+                                              out_z, active, member);
   return cudaGetLastError();
 }
 }  // namespace psv

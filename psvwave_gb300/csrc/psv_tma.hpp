@@ -48,6 +48,9 @@ struct alignas(128) SimDesc {
   // ceil(nz / TZ) tile columns): tile t holds receivers
   // rec_list[rec_start[t] .. rec_start[t + 1]). Used by the persistent step.
   const int *rec_start = nullptr, *rec_list = nullptr;
+  // Position of this simulation's tiles in a batch's tile table (row-major,
+  // tiles_z columns) for the persistent batched step.
+  int tile_base = 0, tiles_x = 0, tiles_z = 0;
 };
 
 // True when tensor-map encoding is available and the row pitch is a
@@ -90,6 +93,14 @@ cudaError_t step_single(const SimDesc &desc, int cfg, bool adjoint, int it, int 
 size_t sched_words(int cfg, int nx, int nz);
 cudaError_t steps_persistent(const SimDesc &desc, int cfg, bool adjoint, int it0, int n_steps,
                              int parity0, bool store, int *err, unsigned *sched, cudaStream_t s);
+// n_steps time steps of every simulation of a batch in one persistent
+// launch, over the batch's tile table (each simulation's tiles contiguous,
+// row-major, at sims[s].tile_base); with `active` non-null only flagged
+// simulations step. sched: sched_words_batch(n_tiles) zeroed words.
+size_t sched_words_batch(int n_tiles);
+cudaError_t steps_persistent_batch(const SimDesc *sims, const int4 *tiles, int n_tiles,
+                                   const int *active, int cfg, int n_steps, bool store, int *err,
+                                   unsigned *sched, cudaStream_t s);
 // Number of tiles of tile shape cfg over an nx x nz grid, and the tile of
 // point (ix, iz).
 int tile_count(int cfg, int nx, int nz);

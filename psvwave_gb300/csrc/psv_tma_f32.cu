@@ -554,6 +554,65 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
   }
 }
 
+// The persistent step over a batch's tile table: items w = step * n_tiles +
+// k for table entries k (simulation, x0, z0, first); neighbours are the
+// tiles of the same simulation around it. Same schedule, waits and
+// publication as fused_steps_tma; inactive simulations' items are skipped
+// (their neighbours are inactive too).
+template <class S, int CFG>
+__global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
+    fused_steps_tma_batch(const SimDesc *__restrict__ sims, const int4 *__restrict__ tiles,
+                          const int *__restrict__ active, int n_tiles, int n_steps, int store,
+                          int *err, unsigned *sched) {
+  __shared__ int s_item;
+  const long long total = (long long)n_steps * n_tiles;
+  uint32_t phase = 0;
+  bool init = true;
+  unsigned next = 0;
+  if (threadIdx.x == 0) next = atomicAdd(sched, 1u);
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = (int)next;
+      next = atomicAdd(sched, 1u);
+    }
+    __syncthreads();
+    const long long w = s_item;
+    __syncthreads();  // everyone has read s_item before thread 0 rewrites it
+    if (w >= total) return;
+    const int j = (int)(w / n_tiles), k = (int)(w - (long long)j * n_tiles);
+    const int4 t = tiles[k];
+    if (active && !active[t.x]) continue;  // uniform: t is the CTA's
+    const SimDesc &d = sims[t.x];
+    const int tx = t.y / S::TX, tz = t.z / S::TZ;
+    if (j > 0) {
+      bool ok = true;
+      if (threadIdx.x < 9) {
+        const int a = tx + (int)threadIdx.x / 3 - 1, b = tz + (int)threadIdx.x % 3 - 1;
+        if (a >= 0 && a < d.tiles_x && b >= 0 && b < d.tiles_z)
+          ok = wait_at_least(sched + 1 + d.tile_base + a * d.tiles_z + b, (unsigned)j);
+      }
+      if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0) atomicOr(err, 2);
+        return;
+      }
+      if (threadIdx.x == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
+    const int parity = j & 1;
+    if (!step_body<S, CFG, false>(d, d.maps[parity], t.y, t.z, false, tx * d.tiles_z + tz, j,
+                                  parity, store, err, phase, init))
+      return;
+    phase ^= 1u;
+    init = false;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + k),
+                   "r"((unsigned)(j + 1))
+                   : "memory");
+    }
+  }
+}
+
 // The shared-memory opt-in is a per-device attribute: set it once per device.
 template <class K>
 cudaError_t configure(K kernel, int smem, unsigned long long &configured) {
@@ -760,6 +819,52 @@ int resident() {
   return per_sm * sms;
 }
 }  // namespace
+
+template <class S, int CFG>
+cudaError_t launch_persistent_batch(const SimDesc *sims, const int4 *tiles, int n_tiles,
+                                    const int *active, int n_steps, int store, int *err,
+                                    unsigned *sched, cudaStream_t s) {
+  static unsigned long long configured = 0;
+  cudaError_t e = configure(fused_steps_tma_batch<S, CFG>, S::SMEM, configured);
+  if (e != cudaSuccess) return e;
+  if (n_steps <= 0 || n_tiles <= 0) return cudaSuccess;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_steps_tma_batch<S, CFG>,
+                                                         S::NT, S::SMEM)) != cudaSuccess)
+    return e;
+  const long long items = (long long)n_steps * n_tiles;
+  const long long slots = (long long)std::max(per_sm, 1) * sms;
+  const int grid = (int)std::min(std::min<long long>(items, slots), 2LL * n_tiles);
+  if (items + grid >= 0x7fffffffLL) return cudaErrorInvalidValue;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(grid);
+  lc.blockDim = dim3(S::NT);
+  lc.dynamicSmemBytes = S::SMEM;
+  lc.stream = s;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, fused_steps_tma_batch<S, CFG>, sims, tiles, active, n_tiles,
+                            n_steps, store, err, sched);
+}
+
+size_t sched_words_batch(int n_tiles) { return 1 + (size_t)std::max(n_tiles, 0); }
+
+cudaError_t steps_persistent_batch(const SimDesc *sims, const int4 *tiles, int n_tiles,
+                                   const int *active, int cfg, int n_steps, bool store, int *err,
+                                   unsigned *sched, cudaStream_t s) {
+  const int st = store ? 1 : 0;
+  if (cfg == kTile16x28)
+    return launch_persistent_batch<Small, kTile16x28>(sims, tiles, n_tiles, active, n_steps, st,
+                                                      err, sched, s);
+  return launch_persistent_batch<Big, kTile32x60>(sims, tiles, n_tiles, active, n_steps, st, err,
+                                                  sched, s);
+}
 
 int resident_ctas(int cfg, bool adjoint) {
   if (cfg == kTile16x28)
