@@ -162,24 +162,32 @@ def fwi_gradients(steps, warmup, with_cpu):
 
     p = workloads.c0_params()
     target, start = workloads.c0_media()
-    m = psv.fdModel.from_parameters(p)
-    m.set_parameter_fields(*target)
-    for s_ in range(m.n_shots):
-        m.forward_simulate(s_, False)
-    m.set_observed_data(*m.get_synthetic_data())
-    m.set_parameter_fields(*start)
-    for _ in range(warmup):
-        m.run_model(False, True)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        m.run_model(False, True)
-        g = m.get_gradient_vector()
-    dt = time.perf_counter() - t0
+
+    def rate(precision):
+        m = psv.fdModel.from_parameters(p, precision=precision)
+        m.set_parameter_fields(*target)
+        for s_ in range(m.n_shots):
+            m.forward_simulate(s_, False)
+        m.set_observed_data(*m.get_synthetic_data())
+        m.set_parameter_fields(*start)
+        for _ in range(warmup):
+            m.run_model(False, True)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            m.run_model(False, True)
+            m.get_gradient_vector()
+        return m, time.perf_counter() - t0
+
+    m, dt = rate("fp32")
+    m64, dt64 = rate("fp64")
     out = {"value": steps / dt, "unit": "FWI gradients/s",
            "workload": "c0: 250x150 grid, nt=4000, 2 sources in 1 shot, 19 receivers, "
                        "snapshot interval 10; forward + misfit + adjoint + kernels per gradient",
            "ms_per_gradient": 1e3 * dt / steps, "misfit": m.misfit,
-           "tile_shape": m.tile_shape}
+           "tile_shape": m.tile_shape,
+           "fp64": {"value": steps / dt64, "ms_per_gradient": 1e3 * dt64 / steps,
+                    "misfit": m64.misfit,
+                    "note": "the reference's precision, bit-identical to it"}}
     if with_cpu:
         from oracle import portbind
         o = portbind.OracleModel(params=p)
