@@ -36,6 +36,7 @@
 #include <cuda_runtime.h>
 
 #include "psv_solver.hpp"
+#include "psv_pdl.cuh"
 
 namespace psv {
 namespace exact {
@@ -89,6 +90,7 @@ __device__ __forceinline__ T at(const AdjArgs<T> &a, const T *f, int x, int z) {
 // w = b dt T lv, once per point (each is used at 9 stencil points).
 template <typename T>
 __global__ void w_fields(AdjArgs<T> a) {
+  kern::pdl_wait();
   const int iz = blockIdx.x * blockDim.x + threadIdx.x;
   const int ix = blockIdx.y * blockDim.y + threadIdx.y;
   if (ix >= a.nx || iz >= a.nz) return;
@@ -103,6 +105,7 @@ __device__ __forceinline__ void pq_at(const AdjArgs<T> &a, int ix, int iz, T &px
 
 template <typename T>
 __global__ void pq_fields(AdjArgs<T> a) {
+  kern::pdl_wait();
   const int iz = blockIdx.x * blockDim.x + threadIdx.x;
   const int ix = blockIdx.y * blockDim.y + threadIdx.y;
   if (ix >= a.nx || iz >= a.nz) return;
@@ -117,6 +120,7 @@ __global__ void pq_fields(AdjArgs<T> a) {
 template <typename T>
 __global__ void velocity_transpose(AdjArgs<T> a, InjPlan plan, const double *stf, int nt,
                                    int it, double dt_d) {
+  kern::pdl_wait();
   const int iz = blockIdx.x * blockDim.x + threadIdx.x;
   const int ix = blockIdx.y * blockDim.y + threadIdx.y;
   if (ix >= a.nx || iz >= a.nz) return;
@@ -188,6 +192,7 @@ __device__ __forceinline__ void pq_at(const AdjArgs<T> &a, int ix, int iz, T &px
 
 template <typename T>
 __global__ void stress_transpose(AdjArgs<T> a) {
+  kern::pdl_wait();
   const int iz = blockIdx.x * blockDim.x + threadIdx.x;
   const int ix = blockIdx.y * blockDim.y + threadIdx.y;
   if (ix >= a.nx || iz >= a.nz) return;
@@ -242,6 +247,7 @@ template <typename T>
 __global__ void add_receiver_terms(int n_groups, int nt, int it, const int *cells,
                                    const int *start, const int *order, const double *adj_x,
                                    const double *adj_z, T *lvx, T *lvz) {
+  kern::pdl_wait();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= 2 * n_groups) return;
   const int grp = k >> 1, comp = k & 1;
@@ -296,15 +302,18 @@ __global__ void add_receiver_terms(int n_groups, int nt, int it, const int *cell
     a.pz = (T *)e.scratch[3];                                                                 \
     a.qq = (T *)e.scratch[4];                                                                 \
     const dim3 block(32, 8), grid((e.nz + 31) / 32, (e.nx + 7) / 8);                          \
-    exact::w_fields<T><<<grid, block, 0, s>>>(a);                                             \
-    exact::velocity_transpose<T><<<grid, block, 0, s>>>(a, e.plan, e.stf, e.nt, e.it, e.dt);  \
-    exact::pq_fields<T><<<grid, block, 0, s>>>(a);                                            \
-    exact::stress_transpose<T><<<grid, block, 0, s>>>(a);                                     \
-    if (e.n_rec_groups)                                                                       \
-      exact::add_receiver_terms<T><<<(2 * e.n_rec_groups + 127) / 128, 128, 0, s>>>(         \
-          e.n_rec_groups, e.nt, e.it, e.rec_cell, e.rec_start, e.rec_order, e.adj_x, e.adj_z, \
-          a.lvx, a.lvz);                                                                      \
-    return cudaGetLastError();                                                                \
+    cudaError_t le = kern::launch_pdl(exact::w_fields<T>, grid, block, s, a);                   \
+    if (le == cudaSuccess)                                                                    \
+      le = kern::launch_pdl(exact::velocity_transpose<T>, grid, block, s, a, e.plan, e.stf,   \
+                            e.nt, e.it, e.dt);                                                \
+    if (le == cudaSuccess) le = kern::launch_pdl(exact::pq_fields<T>, grid, block, s, a);      \
+    if (le == cudaSuccess) le = kern::launch_pdl(exact::stress_transpose<T>, grid, block, s, a); \
+    if (le == cudaSuccess && e.n_rec_groups)                                                  \
+      le = kern::launch_pdl(exact::add_receiver_terms<T>,                                     \
+                            dim3((2 * e.n_rec_groups + 127) / 128), dim3(128), s,              \
+                            e.n_rec_groups, e.nt, e.it, e.rec_cell, e.rec_start, e.rec_order, \
+                            e.adj_x, e.adj_z, a.lvx, a.lvz);                                  \
+    return le;                                                                                \
   }                                                                                           \
   }
 

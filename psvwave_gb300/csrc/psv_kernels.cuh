@@ -25,6 +25,8 @@
 namespace psv {
 namespace kern {
 
+
+
 // Wave-field and medium arrays are stored with a row pitch (pitch >= nz,
 // a multiple of 4 points so rows start on 16-byte boundaries); snapshots,
 // kernels and injection cells use the reference's unpadded [nx][nz] index.
