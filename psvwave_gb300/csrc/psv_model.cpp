@@ -548,7 +548,6 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
   for (auto &b : kexact_) ensure(b, g * sizeof(double));
   for (auto &b : adj_) ensure(b, data_size() * sizeof(double));
   for (auto &b : lam_) ensure(b, gp * e);
-  for (auto &b : exs_) ensure(b, gp * e);
   ensure(ckpt_, n_ck * state_bytes);
   ensure(slots_, (C + 1) * state_bytes);
   if (grown) clear_graphs();
@@ -657,6 +656,8 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
                                       s),
                  "receiver terms");
     for (auto &b : lam_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "zero adjoint");
+    void *lv[2] = {lam_[0].get(), lam_[1].get()};
+    void *ov[2] = {lam_[8].get(), lam_[9].get()};
     void *lt[3] = {lam_[2].get(), lam_[3].get(), lam_[4].get()};
     void *ot[3] = {lam_[5].get(), lam_[6].get(), lam_[7].get()};
     for (int k = n_ck - 1; k >= 0; --k) {
@@ -695,8 +696,10 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
         x.mu = mu_.get();
         x.b = b_.get();
         x.taper_tab = taper_tab_d_.get();
-        x.lv[0] = lam_[0].get();
-        x.lv[1] = lam_[1].get();
+        for (int f = 0; f < 2; ++f) {
+          x.lv[f] = lv[f];
+          x.ov[f] = ov[f];
+        }
         for (int f = 0; f < 3; ++f) {
           x.lt[f] = lt[f];
           x.ot[f] = ot[f];
@@ -718,13 +721,11 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
         x.n_rec_groups = n_rec_groups_;
         x.rec_start = rec_start_.as<int>();
         x.rec_order = rec_order_.as<int>();
-        for (int f = 0; f < 5; ++f) x.scratch[f] = exs_[f].get();
         x.adj_x = adj_[0].as<double>() + off;
         x.adj_z = adj_[1].as<double>() + off;
         cuda_check(prec_ == PSV_FP64 ? exact_step_f64(x, s) : exact_step_f32(x, s), "exact step");
-        std::swap(lt[0], ot[0]);
-        std::swap(lt[1], ot[1]);
-        std::swap(lt[2], ot[2]);
+        for (int f = 0; f < 2; ++f) std::swap(lv[f], ov[f]);
+        for (int f = 0; f < 3; ++f) std::swap(lt[f], ot[f]);
       }
     }
   };

@@ -256,8 +256,7 @@ class Model {
   DeviceBuffer err_flag_;                     // int, raised by bounded device waits
   // exact adjoint: FP64 gradients wrt (lm, la, mu, b) and (vp, vs, rho),
   // receiver terms, adjoint state (lv x2, lt x3, ot x3), checkpoints, slots
-  DeviceBuffer gex_[4], kexact_[3], adj_[2], lam_[8], ckpt_, slots_;
-  DeviceBuffer exs_[5];  // exact adjoint: per-point w and p, q fields
+  DeviceBuffer gex_[4], kexact_[3], adj_[2], lam_[10], ckpt_, slots_;
   // Injection plans: one per shot (sources) and one for the adjoint receivers.
   std::vector<DeviceBuffer> plan_terms_, plan_maps_;
   std::vector<InjPlan> plans_;  // [n_shots] forward, [n_shots] = adjoint

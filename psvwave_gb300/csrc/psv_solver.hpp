@@ -102,8 +102,10 @@ struct ExactStepArgs {
   int nx = 0, nz = 0, pitch = 0, np = 0, nt = 0, it = 0, nr = 0;
   double dt = 0, dx = 0, dz = 0;
   const void *lm = nullptr, *la = nullptr, *mu = nullptr, *b = nullptr, *taper_tab = nullptr;
-  void *lv[2] = {nullptr, nullptr};
-  void *lt[3] = {nullptr, nullptr, nullptr};
+  // adjoint state: l^{n+1} in (lv, lt), l^n out (ov, ot)
+  const void *lv[2] = {nullptr, nullptr};
+  const void *lt[3] = {nullptr, nullptr, nullptr};
+  void *ov[2] = {nullptr, nullptr};
   void *ot[3] = {nullptr, nullptr, nullptr};
   const void *fv[2] = {nullptr, nullptr};
   const void *ft[3] = {nullptr, nullptr, nullptr};
@@ -116,7 +118,6 @@ struct ExactStepArgs {
   int n_rec_groups = 0;
   const int *rec_start = nullptr, *rec_order = nullptr;
   const double *adj_x = nullptr, *adj_z = nullptr;  // receiver terms [nr][nt] of the shot
-  void *scratch[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // padded grids
 };
 cudaError_t exact_step_f32(const ExactStepArgs &e, cudaStream_t s);
 cudaError_t exact_step_f64(const ExactStepArgs &e, cudaStream_t s);
