@@ -31,6 +31,7 @@ UNITS = [
     ("psv_solver_f32.cu", []),
     ("psv_fast_f32.cu", []),
     ("psv_tma_f32.cu", []),
+    ("psv_exact_tma.cu", []),
     ("psv_aux.cu", ["-fmad=false"]),
     ("psv_noalloc.cu", []),
     ("psv_config.cpp", []),

@@ -14,6 +14,7 @@
 #include <sstream>
 
 #include "../../include/psvwave.h"
+#include "psv_exact_tma.hpp"
 #include "psv_fast.hpp"
 
 namespace psv {
@@ -260,6 +261,24 @@ void Model::allocate() {
       cuda_check(cudaMemcpy(rec_order_.get(), order.data(), order.size() * sizeof(int),
                             cudaMemcpyHostToDevice),
                  "upload receiver groups");
+  }
+  {
+    // Receivers by tile of the exact adjoint's TMA step, increasing index
+    // within a tile.
+    const int n_tiles = exact_tma::tile_count(geo_.nx, geo_.nz);
+    std::vector<int> start(n_tiles + 1, 0), list(std::max(cfg_.nr, 1));
+    for (int r = 0; r < cfg_.nr; ++r) ++start[1 + exact_tma::tile_of(geo_.nz, ix_rec_[r], iz_rec_[r])];
+    for (int t = 0; t < n_tiles; ++t) start[t + 1] += start[t];
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int r = 0; r < cfg_.nr; ++r) list[fill[exact_tma::tile_of(geo_.nz, ix_rec_[r], iz_rec_[r])]++] = r;
+    exrec_start_.allocate(start.size() * sizeof(int));
+    exrec_list_.allocate(list.size() * sizeof(int));
+    cuda_check(cudaMemcpy(exrec_start_.get(), start.data(), start.size() * sizeof(int),
+                          cudaMemcpyHostToDevice),
+               "upload receiver tiles");
+    cuda_check(cudaMemcpy(exrec_list_.get(), list.data(), list.size() * sizeof(int),
+                          cudaMemcpyHostToDevice),
+               "upload receiver tiles");
   }
   taper_tab_d_.allocate(taper_tab_.size() * e);
   if (prec_ == PSV_FP64) {
@@ -547,11 +566,20 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
   for (auto &b : gex_) ensure(b, g * sizeof(double));
   for (auto &b : kexact_) ensure(b, g * sizeof(double));
   for (auto &b : adj_) ensure(b, data_size() * sizeof(double));
-  for (auto &b : lam_) ensure(b, gp * e);
+  ensure(lam_, kLamPlanes * field_bytes);
   ensure(ckpt_, n_ck * state_bytes);
   ensure(slots_, (C + 1) * state_bytes);
   if (grown) clear_graphs();
   for (auto &b : gex_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "exact zero");
+  // FP32: the exact step reads its tiles through tensor maps over the
+  // adjoint planes, the state slots and the medium.
+  const bool etma = prec_ == PSV_FP32 && tma_ok_;
+  exact_tma::Maps emaps;
+  if (etma &&
+      !exact_tma::encode(emaps, lam_.as<float>(), kLamPlanes, slots_.as<float>(), 5 * (C + 1),
+                         field_bytes, lm_.as<float>(), la_.as<float>(), mu_.as<float>(),
+                         b_.as<float>(), geo_.nx, geo_.nz, pitch_))
+    throw Error(PSV_ERR_CUDA, "tensor-map encoding failed for the exact adjoint");
 
   const SolverArgs a = solver_args();
   unsigned char *ck = ckpt_.as<unsigned char>(), *sl = slots_.as<unsigned char>();
@@ -655,11 +683,11 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
                                       rtf_true_[c].as<double>() + off, adj_[c].as<double>() + off,
                                       s),
                  "receiver terms");
-    for (auto &b : lam_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "zero adjoint");
-    void *lv[2] = {lam_[0].get(), lam_[1].get()};
-    void *ov[2] = {lam_[8].get(), lam_[9].get()};
-    void *lt[3] = {lam_[2].get(), lam_[3].get(), lam_[4].get()};
-    void *ot[3] = {lam_[5].get(), lam_[6].get(), lam_[7].get()};
+    cuda_check(cudaMemsetAsync(lam_.get(), 0, lam_.bytes(), s), "zero adjoint");
+    // Adjoint state planes: l^{n+1} in (lv, lt), l^n out (ov, ot), swapped
+    // after every step.
+    int lv[2] = {0, 1}, ov[2] = {8, 9}, lt[3] = {2, 3, 4}, ot[3] = {5, 6, 7};
+    auto plane = [&](int k) { return lam_.as<unsigned char>() + k * field_bytes; };
     for (int k = n_ck - 1; k >= 0; --k) {
       const int s0 = k * C, s1 = std::min(nt, s0 + C);
       void *src[5], *slot0[5];
@@ -680,6 +708,46 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
         }
       }
       for (int n = s1 - 1; n >= s0; --n) {
+        if (etma) {
+          exact_tma::Step x;
+          x.nx = geo_.nx;
+          x.nz = geo_.nz;
+          x.pitch = pitch_;
+          x.np = cfg_.np_boundary;
+          x.nt = nt;
+          x.it = n;
+          x.dt = static_cast<float>(cfg_.dt);
+          x.idx = static_cast<float>(1.0 / cfg_.dx);
+          x.idz = static_cast<float>(1.0 / cfg_.dz);
+          x.dt_d = cfg_.dt;
+          x.taper_tab = taper_tab_d_.as<float>();
+          for (int f = 0; f < 2; ++f) {
+            x.lv[f] = lv[f];
+            x.olv[f] = reinterpret_cast<float *>(plane(ov[f]));
+          }
+          for (int f = 0; f < 3; ++f) {
+            x.lt[f] = lt[f];
+            x.olt[f] = reinterpret_cast<float *>(plane(ot[f]));
+          }
+          x.sv = 5 * (n - s0);
+          x.st = 5 * (n + 1 - s0);
+          x.g_lm = gex_[0].as<double>();
+          x.g_la = gex_[1].as<double>();
+          x.g_mu = gex_[2].as<double>();
+          x.g_b = gex_[3].as<double>();
+          x.plan = plans_[shot];
+          x.stf = stf_d_.as<double>();
+          x.rec_cell = rec_cell_.as<int>();
+          x.rec_start = exrec_start_.as<int>();
+          x.rec_list = exrec_list_.as<int>();
+          x.adj_x = adj_[0].as<double>() + off;
+          x.adj_z = adj_[1].as<double>() + off;
+          x.err = err_flag_.as<int>();
+          cuda_check(exact_tma::step(emaps, x, s), "exact step");
+          for (int f = 0; f < 2; ++f) std::swap(lv[f], ov[f]);
+          for (int f = 0; f < 3; ++f) std::swap(lt[f], ot[f]);
+          continue;
+        }
         ExactStepArgs x;
         x.nx = geo_.nx;
         x.nz = geo_.nz;
@@ -697,12 +765,12 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
         x.b = b_.get();
         x.taper_tab = taper_tab_d_.get();
         for (int f = 0; f < 2; ++f) {
-          x.lv[f] = lv[f];
-          x.ov[f] = ov[f];
+          x.lv[f] = plane(lv[f]);
+          x.ov[f] = plane(ov[f]);
         }
         for (int f = 0; f < 3; ++f) {
-          x.lt[f] = lt[f];
-          x.ot[f] = ot[f];
+          x.lt[f] = plane(lt[f]);
+          x.ot[f] = plane(ot[f]);
         }
         const unsigned char *sv = sl + (n - s0) * state_bytes;      // v^n
         const unsigned char *st = sl + (n + 1 - s0) * state_bytes;  // tau^(n+1)
@@ -761,7 +829,7 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
                          kexact_[2].as<double>(), s),
              "exact chain");
   synchronize();
-  if (tma) check_device_error();
+  if (tma || etma) check_device_error();
   return misfit;
 }
 

@@ -256,7 +256,12 @@ class Model {
   DeviceBuffer err_flag_;                     // int, raised by bounded device waits
   // exact adjoint: FP64 gradients wrt (lm, la, mu, b) and (vp, vs, rho),
   // receiver terms, adjoint state (lv x2, lt x3, ot x3), checkpoints, slots
-  DeviceBuffer gex_[4], kexact_[3], adj_[2], lam_[10], ckpt_, slots_;
+  // Exact adjoint: FP64 gradient sums, outputs, receiver terms, adjoint
+  // state planes (lv in/out: 0-1 / 8-9, lt in/out: 2-4 / 5-7), checkpoints
+  // and state slots.
+  static constexpr int kLamPlanes = 10;
+  DeviceBuffer gex_[4], kexact_[3], adj_[2], lam_, ckpt_, slots_;
+  DeviceBuffer exrec_start_, exrec_list_;  // receivers by tile of the exact TMA step
   // Injection plans: one per shot (sources) and one for the adjoint receivers.
   std::vector<DeviceBuffer> plan_terms_, plan_maps_;
   std::vector<InjPlan> plans_;  // [n_shots] forward, [n_shots] = adjoint

@@ -57,6 +57,13 @@ struct alignas(128) SimDesc {
 // multiple of 4 points (16-byte rows).
 bool supported(int nx, int nz, int pitch);
 
+// A 2-D tensor map over an [nx][pitch] float array (nz valid columns) with
+// width x rows boxes; a 3-D one over `planes` such arrays plane_bytes apart
+// (boxes one plane deep). False on failure.
+bool encode_2d(CUtensorMap *m, const float *ptr, int nx, int nz, int pitch, int width, int rows);
+bool encode_planes(CUtensorMap *m, const float *base, int planes, size_t plane_bytes, int nx,
+                   int nz, int pitch, int width, int rows);
+
 // Encodes desc.maps for tile shape `cfg` from desc.set, desc.lm and the mu
 // array; false on failure.
 bool make_maps(SimDesc &desc, const float *mu, int cfg);

@@ -31,6 +31,7 @@
 #include <cstdint>
 
 #include "psv_tma.hpp"
+#include "psv_tma_ptx.cuh"
 
 namespace psv {
 namespace tma {
@@ -59,37 +60,6 @@ struct Shape {
 };
 using Big = Shape<32, 60, 256>;
 using Small = Shape<16, 28, 128>;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1,
-                                            uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Bounded wait on phase `parity`: true when the phase completed. Each try
-// suspends for at most about 1 us.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t max_iter) {
-  const uint32_t addr = smem_u32(bar);
-  for (uint32_t i = 0; i < max_iter; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n"
-        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
-        " selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(addr), "r"(parity), "r"(1000u)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
 
 __device__ __forceinline__ void correlate(const SimDesc &d, const float *const asnap[5], int g,
                                           float lm, float mu, float vx, float vz, float txx,
@@ -130,14 +100,6 @@ __device__ __forceinline__ void inject(const SimDesc &d, int it, int g, int gx, 
   }
 }
 
-// Programmatic dependent launch: a step launched with programmatic stream
-// serialisation may start while the previous step drains; griddep_wait
-// returns once that step has completed and its writes are visible (a no-op
-// for launches without the attribute).
-__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void griddep_launch_dependents() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
 
 // An interior tile computes every stress point of its box (rows X0-2 ..
 // X0+TX+1, columns Z0-2 .. Z0+TZ+1) inside the updated region 2 <= x < n-2
@@ -744,6 +706,24 @@ bool encode_set(Maps &m, const fast::Fields &f, const float *lm, const float *mu
 }
 
 }  // namespace
+
+bool encode_2d(CUtensorMap *m, const float *ptr, int nx, int nz, int pitch, int width, int rows) {
+  return encode(m, ptr, nx, nz, pitch, width, rows);
+}
+
+bool encode_planes(CUtensorMap *m, const float *base, int planes, size_t plane_bytes, int nx,
+                   int nz, int pitch, int width, int rows) {
+  EncodeTiled fn = encoder();
+  if (!fn || plane_bytes % 16 != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nz, (cuuint64_t)nx, (cuuint64_t)planes};
+  const cuuint64_t strides[2] = {(cuuint64_t)pitch * sizeof(float), (cuuint64_t)plane_bytes};
+  const cuuint32_t box[3] = {(cuuint32_t)width, (cuuint32_t)rows, 1};
+  const cuuint32_t elem[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box,
+            elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
 
 void tile_dims(int cfg, int *tx, int *tz) {
   *tx = cfg == kTile16x28 ? Small::TX : Big::TX;
