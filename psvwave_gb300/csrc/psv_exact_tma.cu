@@ -3,7 +3,7 @@
 // The transpose of the forward step (notation and algebra in psv_exact.cuh):
 // per step n, from l^{n+1} = (lv, lt), the forward states v^n and tau^{n+1}
 // and the medium, it produces l^n = (v-bar, tau-bar) and adds the step's
-// terms to the FP64 gradients of lm, la, mu and b. Each CTA owns a
+// terms to the gradients of lm, la, mu and b. Each CTA owns a
 // kTX x kTZ tile. Thread 0 issues fourteen tiled bulk-tensor copies that
 // complete on one mbarrier: b, lv with a 4-point halo in both axes; lt, lm,
 // la, mu, v^n and tau^{n+1} with a 2-point halo (all boxes kTZ + 8 wide,
@@ -15,15 +15,22 @@
 //   phase 2: lt~ = lt + A^T w (in place) and p = dt C y over the tile + 2;
 //   phase 3: per own point, tau-bar = T lt~, v-bar = T lv + E^T p plus the
 //            receiver terms of the point (in increasing receiver index), and
-//            the gradient terms, added to values loaded right after the wait.
-// Every expression and every FP64 accumulation order is that of
-// exact::exact_step_tile<float> followed by exact::add_receiver_terms, so
-// both give the same bits.
+//            the gradient terms, added to sums loaded right after the wait.
+// The adjoint state is computed with exactly the expressions of
+// exact::exact_step_tile<float> and exact::add_receiver_terms (the same
+// bits). The gradient terms are formed in FP32 and summed in float-float
+// pairs (hi, lo) with Knuth's TwoSum (The Art of Computer Programming,
+// vol. 2, 4.2.2), which carries each addition's rounding error exactly into
+// lo: about 48 significant bits, like the FP64 sums of exact_step_tile, but
+// on the FP32 pipes (GB300 issues FP64 at a small fraction of the FP32
+// rate, and FP64 sums were most of this kernel's time). finish() turns the
+// pairs into FP64 once per gradient.
 //
 // The mbarrier wait is bounded: on time-out the CTA raises the error flag,
 // waits (bounded again) for its copies to land, and returns.
 #include "psv_exact_tma.hpp"
 
+#include <algorithm>
 #include <cstdint>
 
 #include "psv_tma.hpp"
@@ -70,6 +77,15 @@ __device__ __forceinline__ bool interior(const Step &a, int ix, int iz) {
   return ix >= 2 && ix < a.nx - 2 && iz >= 2 && iz < a.nz - 2;
 }
 
+// (hi, lo) + x: s = hi + x rounded, and e with s + e == hi + x exactly
+// (TwoSum); e goes into lo.
+__device__ __forceinline__ float2 ff_add(float2 a, float x) {
+  const float s = a.x + x;
+  const float bp = s - a.x;
+  const float e = (a.x - (s - bp)) + (x - bp);
+  return make_float2(s, a.y + e);
+}
+
 __global__ void __launch_bounds__(NT)
     exact_step_tma(const __grid_constant__ Maps maps, const Step a, int tiles_z) {
   extern __shared__ unsigned char smem_raw[];
@@ -111,11 +127,11 @@ __global__ void __launch_bounds__(NT)
   // gradient sums, loaded while the copies fly.
   const int lane = tid & 31, wr = tid >> 5;
   const int iz = Z0 + lane;
-  double glm[ROWS], gla[ROWS], gmu[ROWS], gb[ROWS];
+  float2 glm[ROWS], gla[ROWS], gmu[ROWS], gb[ROWS];
 #pragma unroll
   for (int j = 0; j < ROWS; ++j) {
     const int ix = X0 + wr + j * (NT / 32);
-    glm[j] = gla[j] = gmu[j] = gb[j] = 0.0;
+    glm[j] = gla[j] = gmu[j] = gb[j] = make_float2(0.f, 0.f);
     if (ix < a.nx && iz < a.nz) {
       const size_t u = (size_t)ix * a.nz + iz;
       glm[j] = a.g_lm[u];
@@ -232,24 +248,23 @@ __global__ void __launch_bounds__(NT)
     }
     a.olv[0][p] = ovx;
     a.olv[1][p] = ovz;
-    double g_b = gb[j];
+    float2 g_b = gb[j];
     if (in) {
       // grad_b += dt T lv . A tau^{n+1}
       const float ax = (c1 * (FXX[s] - FXX[s - W]) + c2 * (FXX[s - 2 * W] - FXX[s + W])) * a.idx +
                        (c1 * (FXZ[s] - FXZ[s - 1]) + c2 * (FXZ[s - 2] - FXZ[s + 1])) * a.idz;
       const float az = (c1 * (FXZ[s + W] - FXZ[s]) + c2 * (FXZ[s - W] - FXZ[s + 2 * W])) * a.idx +
                        (c1 * (FZZ[s + 1] - FZZ[s]) + c2 * (FZZ[s - 1] - FZZ[s + 2])) * a.idz;
-      g_b += (double)(a.dt * tp) * ((double)lvx * (double)ax + (double)lvz * (double)az);
+      g_b = ff_add(g_b, (a.dt * tp) * (lvx * ax + lvz * az));
       // Medium gradients from the strain rates of v^n.
       const float ex = (c1 * (FVX[s + W] - FVX[s]) + c2 * (FVX[s - W] - FVX[s + 2 * W])) * a.idx;
       const float ez = (c1 * (FVZ[s] - FVZ[s - 1]) + c2 * (FVZ[s - 2] - FVZ[s + 1])) * a.idz;
       const float gxz = (c1 * (FVX[s + 1] - FVX[s]) + c2 * (FVX[s - 1] - FVX[s + 2])) * a.idz +
                         (c1 * (FVZ[s] - FVZ[s - W]) + c2 * (FVZ[s - 2 * W] - FVZ[s + W])) * a.idx;
-      const double yxx = (double)(tp * lxx), yzz = (double)(tp * lzz), yxz = (double)(tp * lxz);
-      const double dt = (double)a.dt;
-      a.g_lm[u] = glm[j] + dt * (yxx * (double)ex + yzz * (double)ez);
-      a.g_la[u] = gla[j] + dt * (yxx * (double)ez + yzz * (double)ex);
-      a.g_mu[u] = gmu[j] + dt * yxz * (double)gxz;
+      const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
+      a.g_lm[u] = ff_add(glm[j], a.dt * (yxx * ex + yzz * ez));
+      a.g_la[u] = ff_add(gla[j], a.dt * (yxx * ez + yzz * ex));
+      a.g_mu[u] = ff_add(gmu[j], a.dt * yxz * gxz);
     }
     // Source terms s = coef stf dt b / div at their points depend on b.
     const InjPlan &pl = a.plan;
@@ -260,7 +275,7 @@ __global__ void __launch_bounds__(NT)
         const InjTerm t = pl.terms[k];
         if (t.kind != 0) continue;
         const double ds = ((t.coef * a.stf[(size_t)t.index * a.nt + a.it]) * a.dt_d) / t.div;
-        g_b += ds * (double)(t.field == 0 ? lvx : lvz);
+        g_b = ff_add(g_b, (float)(ds * (double)(t.field == 0 ? lvx : lvz)));
         src = true;
       }
     }
@@ -284,6 +299,24 @@ bool encode(Maps &m, const float *lam, int n_lam, const float *slots, int n_slot
          tma::encode_2d(&m.la, la, nx, nz, pitch, W, SR) &&
          tma::encode_2d(&m.mu, mu, nx, nz, pitch, W, SR) &&
          tma::encode_2d(&m.b, b, nx, nz, pitch, W, VR);
+}
+
+__global__ void ff_finish(size_t n, const float2 *a0, const float2 *a1, const float2 *a2,
+                          const float2 *a3, double *o0, double *o1, double *o2, double *o3) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    o0[i] = (double)a0[i].x + (double)a0[i].y;
+    o1[i] = (double)a1[i].x + (double)a1[i].y;
+    o2[i] = (double)a2[i].x + (double)a2[i].y;
+    o3[i] = (double)a3[i].x + (double)a3[i].y;
+  }
+}
+
+cudaError_t finish(size_t n, float2 *const ff[4], double *const out[4], cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+  ff_finish<<<blocks, 256, 0, s>>>(n, ff[0], ff[1], ff[2], ff[3], out[0], out[1], out[2], out[3]);
+  return cudaGetLastError();
 }
 
 cudaError_t step(const Maps &maps, const Step &a, cudaStream_t s) {

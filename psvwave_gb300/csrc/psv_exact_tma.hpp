@@ -25,7 +25,8 @@ struct Maps {
 
 // One step n: reads l^{n+1} from planes lv[], lt[] and the forward states
 // v^n (slot planes sv, sv + 1) and tau^{n+1} (slot planes st + 2 .. st + 4);
-// writes l^n to olv[], olt[] (padded grids) and adds to the FP64 gradients.
+// writes l^n to olv[], olt[] (padded grids) and adds the step's terms to
+// the gradient sums, float-float pairs (hi, lo) over the unpadded grid.
 struct Step {
   int nx = 0, nz = 0, pitch = 0, np = 0, nt = 0, it = 0;
   float dt = 0, idx = 0, idz = 0;
@@ -34,7 +35,7 @@ struct Step {
   int lv[2] = {0, 0}, lt[3] = {0, 0, 0}, sv = 0, st = 0;
   float *olv[2] = {nullptr, nullptr};
   float *olt[3] = {nullptr, nullptr, nullptr};
-  double *g_lm = nullptr, *g_la = nullptr, *g_mu = nullptr, *g_b = nullptr;
+  float2 *g_lm = nullptr, *g_la = nullptr, *g_mu = nullptr, *g_b = nullptr;
   InjPlan plan{};
   const double *stf = nullptr;
   // Receivers by tile (tiles row-major over ceil(nz / kTZ) columns): tile t
@@ -56,6 +57,9 @@ int tile_of(int nz, int ix, int iz);
 int tile_count(int nx, int nz);
 
 cudaError_t step(const Maps &maps, const Step &a, cudaStream_t s);
+
+// out[k][i] = hi + lo of the pair ff[k][i] in FP64, k = 0..3, i < n.
+cudaError_t finish(size_t n, float2 *const ff[4], double *const out[4], cudaStream_t s);
 
 }  // namespace exact_tma
 }  // namespace psv

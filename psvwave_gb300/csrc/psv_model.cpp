@@ -567,13 +567,18 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
   for (auto &b : kexact_) ensure(b, g * sizeof(double));
   for (auto &b : adj_) ensure(b, data_size() * sizeof(double));
   ensure(lam_, kLamPlanes * field_bytes);
+  const bool etma = prec_ == PSV_FP32 && tma_ok_;
+  if (etma)
+    for (auto &b : gff_) ensure(b, g * sizeof(float2));
   ensure(ckpt_, n_ck * state_bytes);
   ensure(slots_, (C + 1) * state_bytes);
   if (grown) clear_graphs();
   for (auto &b : gex_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "exact zero");
+  if (etma)
+    for (auto &b : gff_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), s), "exact zero");
   // FP32: the exact step reads its tiles through tensor maps over the
-  // adjoint planes, the state slots and the medium.
-  const bool etma = prec_ == PSV_FP32 && tma_ok_;
+  // adjoint planes, the state slots and the medium, and sums the gradient
+  // in float-float pairs (gff_), turned into FP64 (gex_) at the end.
   exact_tma::Maps emaps;
   if (etma &&
       !exact_tma::encode(emaps, lam_.as<float>(), kLamPlanes, slots_.as<float>(), 5 * (C + 1),
@@ -731,10 +736,10 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
           }
           x.sv = 5 * (n - s0);
           x.st = 5 * (n + 1 - s0);
-          x.g_lm = gex_[0].as<double>();
-          x.g_la = gex_[1].as<double>();
-          x.g_mu = gex_[2].as<double>();
-          x.g_b = gex_[3].as<double>();
+          x.g_lm = gff_[0].as<float2>();
+          x.g_la = gff_[1].as<float2>();
+          x.g_mu = gff_[2].as<float2>();
+          x.g_b = gff_[3].as<float2>();
           x.plan = plans_[shot];
           x.stf = stf_d_.as<double>();
           x.rec_cell = rec_cell_.as<int>();
@@ -821,6 +826,13 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
       misfit += v;
     }
     misfit_ = misfit;
+  }
+  if (etma) {
+    float2 *ff[4] = {gff_[0].as<float2>(), gff_[1].as<float2>(), gff_[2].as<float2>(),
+                     gff_[3].as<float2>()};
+    double *out[4] = {gex_[0].as<double>(), gex_[1].as<double>(), gex_[2].as<double>(),
+                      gex_[3].as<double>()};
+    cuda_check(exact_tma::finish(g, ff, out, s), "exact sums");
   }
   // Chain rule to (vp, vs, rho).
   cuda_check(exact_chain(g, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(),

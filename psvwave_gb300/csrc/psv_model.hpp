@@ -262,6 +262,7 @@ class Model {
   static constexpr int kLamPlanes = 10;
   DeviceBuffer gex_[4], kexact_[3], adj_[2], lam_, ckpt_, slots_;
   DeviceBuffer exrec_start_, exrec_list_;  // receivers by tile of the exact TMA step
+  DeviceBuffer gff_[4];  // FP32 exact step: float-float gradient sums (lm, la, mu, b)
   // Injection plans: one per shot (sources) and one for the adjoint receivers.
   std::vector<DeviceBuffer> plan_terms_, plan_maps_;
   std::vector<InjPlan> plans_;  // [n_shots] forward, [n_shots] = adjoint
