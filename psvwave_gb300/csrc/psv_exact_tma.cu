@@ -12,7 +12,8 @@
 // programmatic-dependent-launch wait (it does not change during a gradient),
 // the rest after it. Then, in shared memory:
 //   phase 1: w = b dt T lv over the tile + 4;
-//   phase 2: lt~ = lt + A^T w (in place) and p = dt C y over the tile + 2;
+//   phase 2: lt~ = lt + A^T w (in place) and p = dt C y over the tile + 2
+//            (in place of lm, la, mu: each point reads only its own);
 //   phase 3: per own point, tau-bar = T lt~, v-bar = T lv + E^T p plus the
 //            receiver terms of the point (in increasing receiver index), and
 //            the gradient terms, added to sums loaded right after the wait.
@@ -25,6 +26,10 @@
 // on the FP32 pipes (GB300 issues FP64 at a small fraction of the FP32
 // rate, and FP64 sums were most of this kernel's time). finish() turns the
 // pairs into FP64 once per gradient.
+//
+// Tiles whose 4-halo region lies inside the updated region and at least np
+// frames deep (taper exactly 1) and that hold no source point take a path
+// without per-point tests.
 //
 // The mbarrier wait is bounded: on time-out the CTA raises the error flag,
 // waits (bounded again) for its copies to land, and returns.
@@ -60,8 +65,8 @@ constexpr int OFF_M = OFF_LT + 3 * SB;      // lm, la, mu
 constexpr int OFF_FV = OFF_M + 3 * SB;      // vx, vz of v^n
 constexpr int OFF_FT = OFF_FV + 2 * SB;     // txx, tzz, txz of tau^{n+1}
 constexpr int OFF_W = OFF_FT + 3 * SB;      // wx, wz
-constexpr int OFF_P = OFF_W + 2 * VB;       // px, pz, q
-constexpr int TOTAL = OFF_P + 3 * SB;
+constexpr int OFF_P = OFF_M;                // px, pz, q over lm, la, mu (same points)
+constexpr int TOTAL = OFF_W + 2 * VB;
 constexpr int TX_BYTES = OFF_W * 4;         // delivered by the copies
 constexpr int SMEM = TOTAL * 4 + 16 + 128;  // + mbarrier + alignment slack
 constexpr int ROWS = TX / (NT / 32);        // own rows per thread
@@ -86,6 +91,159 @@ __device__ __forceinline__ float2 ff_add(float2 a, float x) {
   return make_float2(s, a.y + e);
 }
 
+// Phases 1-3 of one tile (the copies have landed). INNER: every point of
+// the 4-halo region is interior with taper 1 and no own point has a source
+// term.
+template <bool INNER>
+__device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int Z0,
+                                          const float2 *glm, const float2 *gla,
+                                          const float2 *gmu, const float2 *gb) {
+  const int tid = threadIdx.x, lane = tid & 31, wr = tid >> 5;
+  const int iz = Z0 + lane;
+  const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
+  const float *LVX = sm + OFF_LV, *LVZ = sm + OFF_LV + VB, *B = sm + OFF_B;
+  float *WX = sm + OFF_W, *WZ = sm + OFF_W + VB;
+  // Phase 1: w = b dt T lv at interior points, 0 elsewhere.
+  for (int k = tid; k < VB; k += NT) {
+    const int r = k / W, c = k - r * W;
+    const int ix = X0 - 4 + r, jz = Z0 - 4 + c;
+    float wx = 0.f, wz = 0.f;
+    if (INNER) {
+      const float s = B[k] * a.dt;
+      wx = s * LVX[k];
+      wz = s * LVZ[k];
+    } else if (ix >= 0 && ix < a.nx && jz >= 0 && jz < a.nz && interior(a, ix, jz)) {
+      const float s = B[k] * a.dt * taper_at(a, ix, jz);
+      wx = s * LVX[k];
+      wz = s * LVZ[k];
+    }
+    WX[k] = wx;
+    WZ[k] = wz;
+  }
+  __syncthreads();
+
+  float *LXX = sm + OFF_LT, *LZZ = sm + OFF_LT + SB, *LXZ = sm + OFF_LT + 2 * SB;
+  const float *LM = sm + OFF_M, *LA = sm + OFF_M + SB, *MU = sm + OFF_M + 2 * SB;
+  float *PX = sm + OFF_P, *PZ = sm + OFF_P + SB, *QQ = sm + OFF_P + 2 * SB;
+  // Phase 2: lt~ = lt - (A^T w terms), and p_x = dt (lm y_xx + la y_zz),
+  // p_z = dt (la y_xx + lm y_zz), q = dt mu y_xz with y = T lt~ on I, 0
+  // elsewhere; over rows X0-2 .. X0+TX+1 and columns Z0-2 .. Z0+TZ+1.
+  for (int k = tid; k < SR * PC; k += NT) {
+    const int r = k / PC, c = 2 + (k - r * PC);
+    const int ix = X0 - 2 + r, jz = Z0 - 4 + c;
+    const int s = r * W + c;        // in the 2-halo boxes
+    const int v = (r + 2) * W + c;  // the same point in the 4-halo boxes
+    float px = 0.f, pz = 0.f, q = 0.f;
+    if (INNER || (ix >= 0 && ix < a.nx && jz >= 0 && jz < a.nz)) {
+      const float dxp_wx = c1 * (WX[v + W] - WX[v]) + c2 * (WX[v - W] - WX[v + 2 * W]);
+      const float dzp_wx = c1 * (WX[v + 1] - WX[v]) + c2 * (WX[v - 1] - WX[v + 2]);
+      const float dzm_wz = c1 * (WZ[v] - WZ[v - 1]) + c2 * (WZ[v - 2] - WZ[v + 1]);
+      const float dxm_wz = c1 * (WZ[v] - WZ[v - W]) + c2 * (WZ[v - 2 * W] - WZ[v + W]);
+      const float lxx = LXX[s] - dxp_wx * a.idx;
+      const float lzz = LZZ[s] - dzm_wz * a.idz;
+      const float lxz = LXZ[s] - dzp_wx * a.idz - dxm_wz * a.idx;
+      LXX[s] = lxx;
+      LZZ[s] = lzz;
+      LXZ[s] = lxz;
+      if (INNER) {
+        const float lm = LM[s], la = LA[s], mu = MU[s];
+        px = a.dt * (lm * lxx + la * lzz);
+        pz = a.dt * (la * lxx + lm * lzz);
+        q = a.dt * mu * lxz;
+      } else if (interior(a, ix, jz)) {
+        const float tp = taper_at(a, ix, jz);
+        const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
+        if (!(yxx == 0.f && yzz == 0.f && yxz == 0.f)) {
+          const float lm = LM[s], la = LA[s], mu = MU[s];
+          px = a.dt * (lm * yxx + la * yzz);
+          pz = a.dt * (la * yxx + lm * yzz);
+          q = a.dt * mu * yxz;
+        }
+      }
+    }
+    PX[s] = px;
+    PZ[s] = pz;
+    QQ[s] = q;
+  }
+  __syncthreads();
+
+  // Phase 3: own points.
+  if (!INNER && iz >= a.nz) return;
+  const float *FVX = sm + OFF_FV, *FVZ = sm + OFF_FV + SB;
+  const float *FXX = sm + OFF_FT, *FZZ = sm + OFF_FT + SB, *FXZ = sm + OFF_FT + 2 * SB;
+  const int tile = blockIdx.x;
+  const int r0 = a.rec_start[tile], r1 = a.rec_start[tile + 1];
+  const int c = lane + 4;
+#pragma unroll
+  for (int j = 0; j < ROWS; ++j) {
+    const int lx = wr + j * (NT / 32);
+    const int ix = X0 + lx;
+    if (!INNER && ix >= a.nx) break;
+    const size_t p = (size_t)ix * a.pitch + iz;
+    const size_t u = (size_t)ix * a.nz + iz;
+    const int s = (lx + 2) * W + c;  // 2-halo boxes
+    const int v = (lx + 4) * W + c;  // 4-halo boxes
+    const bool in = INNER || interior(a, ix, iz);
+    const float tp = (INNER || !in) ? 1.f : taper_at(a, ix, iz);
+    const float lxx = LXX[s], lzz = LZZ[s], lxz = LXZ[s];
+    // tau-bar^n
+    a.olt[0][p] = tp * lxx;
+    a.olt[1][p] = tp * lzz;
+    a.olt[2][p] = tp * lxz;
+    // E^T (dt C y):  v-bar_x += -D-_x(p_x)/dx - D-_z(q)/dz,
+    //                v-bar_z += -D+_z(p_z)/dz - D+_x(q)/dx
+    const float dxm_px = c1 * (PX[s] - PX[s - W]) + c2 * (PX[s - 2 * W] - PX[s + W]);
+    const float dzm_q = c1 * (QQ[s] - QQ[s - 1]) + c2 * (QQ[s - 2] - QQ[s + 1]);
+    const float dzp_pz = c1 * (PZ[s + 1] - PZ[s]) + c2 * (PZ[s - 1] - PZ[s + 2]);
+    const float dxp_q = c1 * (QQ[s + W] - QQ[s]) + c2 * (QQ[s - W] - QQ[s + 2 * W]);
+    const float lvx = LVX[v], lvz = LVZ[v];
+    float ovx = tp * lvx - dxm_px * a.idx - dzm_q * a.idz;
+    float ovz = tp * lvz - dzp_pz * a.idz - dxp_q * a.idx;
+    // Receiver terms v-bar^n(rec) += adj[r][n].
+    for (int i = r0; i < r1; ++i) {
+      const int rr = a.rec_list[i];
+      if (a.rec_cell[rr] == (int)p) {
+        ovx = ovx + (float)a.adj_x[(size_t)rr * a.nt + a.it];
+        ovz = ovz + (float)a.adj_z[(size_t)rr * a.nt + a.it];
+      }
+    }
+    a.olv[0][p] = ovx;
+    a.olv[1][p] = ovz;
+    float2 g_b = gb[j];
+    if (in) {
+      // grad_b += dt T lv . A tau^{n+1}
+      const float ax = (c1 * (FXX[s] - FXX[s - W]) + c2 * (FXX[s - 2 * W] - FXX[s + W])) * a.idx +
+                       (c1 * (FXZ[s] - FXZ[s - 1]) + c2 * (FXZ[s - 2] - FXZ[s + 1])) * a.idz;
+      const float az = (c1 * (FXZ[s + W] - FXZ[s]) + c2 * (FXZ[s - W] - FXZ[s + 2 * W])) * a.idx +
+                       (c1 * (FZZ[s + 1] - FZZ[s]) + c2 * (FZZ[s - 1] - FZZ[s + 2])) * a.idz;
+      g_b = ff_add(g_b, (a.dt * tp) * (lvx * ax + lvz * az));
+      // Medium gradients from the strain rates of v^n.
+      const float ex = (c1 * (FVX[s + W] - FVX[s]) + c2 * (FVX[s - W] - FVX[s + 2 * W])) * a.idx;
+      const float ez = (c1 * (FVZ[s] - FVZ[s - 1]) + c2 * (FVZ[s - 2] - FVZ[s + 1])) * a.idz;
+      const float gxz = (c1 * (FVX[s + 1] - FVX[s]) + c2 * (FVX[s - 1] - FVX[s + 2])) * a.idz +
+                        (c1 * (FVZ[s] - FVZ[s - W]) + c2 * (FVZ[s - 2 * W] - FVZ[s + W])) * a.idx;
+      const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
+      a.g_lm[u] = ff_add(glm[j], a.dt * (yxx * ex + yzz * ez));
+      a.g_la[u] = ff_add(gla[j], a.dt * (yxx * ez + yzz * ex));
+      a.g_mu[u] = ff_add(gmu[j], a.dt * yxz * gxz);
+    }
+    // Source terms s = coef stf dt b / div at their points depend on b.
+    const InjPlan &pl = a.plan;
+    bool src = false;
+    if (!INNER && pl.n && ix >= pl.x0 && ix < pl.x0 + pl.w && iz >= pl.z0 && iz < pl.z0 + pl.h) {
+      int k = pl.map[(ix - pl.x0) * pl.h + (iz - pl.z0)];
+      for (; k >= 0 && k < pl.n && pl.terms[k].cell == (int)u; ++k) {
+        const InjTerm t = pl.terms[k];
+        if (t.kind != 0) continue;
+        const double ds = ((t.coef * a.stf[(size_t)t.index * a.nt + a.it]) * a.dt_d) / t.div;
+        g_b = ff_add(g_b, (float)(ds * (double)(t.field == 0 ? lvx : lvz)));
+        src = true;
+      }
+    }
+    if (in || src) a.g_b[u] = g_b;
+  }
+}
+
 __global__ void __launch_bounds__(NT)
     exact_step_tma(const __grid_constant__ Maps maps, const Step a, int tiles_z) {
   extern __shared__ unsigned char smem_raw[];
@@ -95,7 +253,6 @@ __global__ void __launch_bounds__(NT)
   const int tx = blockIdx.x / tiles_z, tz = blockIdx.x - tx * tiles_z;
   const int X0 = tx * TX, Z0 = tz * TZ;
   const int tid = threadIdx.x;
-  const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
 
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(1)
@@ -150,137 +307,17 @@ __global__ void __launch_bounds__(NT)
     return;
   }
 
-  const float *LVX = sm + OFF_LV, *LVZ = sm + OFF_LV + VB, *B = sm + OFF_B;
-  float *WX = sm + OFF_W, *WZ = sm + OFF_W + VB;
-  // Phase 1: w = b dt T lv at interior points, 0 elsewhere.
-  for (int k = tid; k < VB; k += NT) {
-    const int r = k / W, c = k - r * W;
-    const int ix = X0 - 4 + r, jz = Z0 - 4 + c;
-    float wx = 0.f, wz = 0.f;
-    if (ix >= 0 && ix < a.nx && jz >= 0 && jz < a.nz && interior(a, ix, jz)) {
-      const float s = B[k] * a.dt * taper_at(a, ix, jz);
-      wx = s * LVX[k];
-      wz = s * LVZ[k];
-    }
-    WX[k] = wx;
-    WZ[k] = wz;
-  }
-  __syncthreads();
-
-  float *LXX = sm + OFF_LT, *LZZ = sm + OFF_LT + SB, *LXZ = sm + OFF_LT + 2 * SB;
-  const float *LM = sm + OFF_M, *LA = sm + OFF_M + SB, *MU = sm + OFF_M + 2 * SB;
-  float *PX = sm + OFF_P, *PZ = sm + OFF_P + SB, *QQ = sm + OFF_P + 2 * SB;
-  // Phase 2: lt~ = lt - (A^T w terms), and p_x = dt (lm y_xx + la y_zz),
-  // p_z = dt (la y_xx + lm y_zz), q = dt mu y_xz with y = T lt~ on I, 0
-  // elsewhere; over rows X0-2 .. X0+TX+1 and columns Z0-2 .. Z0+TZ+1.
-  for (int k = tid; k < SR * PC; k += NT) {
-    const int r = k / PC, c = 2 + (k - r * PC);
-    const int ix = X0 - 2 + r, jz = Z0 - 4 + c;
-    const int s = r * W + c;        // in the 2-halo boxes
-    const int v = (r + 2) * W + c;  // the same point in the 4-halo boxes
-    float px = 0.f, pz = 0.f, q = 0.f;
-    if (ix >= 0 && ix < a.nx && jz >= 0 && jz < a.nz) {
-      const float dxp_wx = c1 * (WX[v + W] - WX[v]) + c2 * (WX[v - W] - WX[v + 2 * W]);
-      const float dzp_wx = c1 * (WX[v + 1] - WX[v]) + c2 * (WX[v - 1] - WX[v + 2]);
-      const float dzm_wz = c1 * (WZ[v] - WZ[v - 1]) + c2 * (WZ[v - 2] - WZ[v + 1]);
-      const float dxm_wz = c1 * (WZ[v] - WZ[v - W]) + c2 * (WZ[v - 2 * W] - WZ[v + W]);
-      const float lxx = LXX[s] - dxp_wx * a.idx;
-      const float lzz = LZZ[s] - dzm_wz * a.idz;
-      const float lxz = LXZ[s] - dzp_wx * a.idz - dxm_wz * a.idx;
-      LXX[s] = lxx;
-      LZZ[s] = lzz;
-      LXZ[s] = lxz;
-      if (interior(a, ix, jz)) {
-        const float tp = taper_at(a, ix, jz);
-        const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
-        if (!(yxx == 0.f && yzz == 0.f && yxz == 0.f)) {
-          px = a.dt * (LM[s] * yxx + LA[s] * yzz);
-          pz = a.dt * (LA[s] * yxx + LM[s] * yzz);
-          q = a.dt * MU[s] * yxz;
-        }
-      }
-    }
-    PX[s] = px;
-    PZ[s] = pz;
-    QQ[s] = q;
-  }
-  __syncthreads();
-
-  // Phase 3: own points.
-  if (iz >= a.nz) return;
-  const float *FVX = sm + OFF_FV, *FVZ = sm + OFF_FV + SB;
-  const float *FXX = sm + OFF_FT, *FZZ = sm + OFF_FT + SB, *FXZ = sm + OFF_FT + 2 * SB;
-  const int tile = blockIdx.x;
-  const int r0 = a.rec_start[tile], r1 = a.rec_start[tile + 1];
-  const int c = lane + 4;
-#pragma unroll
-  for (int j = 0; j < ROWS; ++j) {
-    const int lx = wr + j * (NT / 32);
-    const int ix = X0 + lx;
-    if (ix >= a.nx) break;
-    const size_t p = (size_t)ix * a.pitch + iz;
-    const size_t u = (size_t)ix * a.nz + iz;
-    const int s = (lx + 2) * W + c;  // 2-halo boxes
-    const int v = (lx + 4) * W + c;  // 4-halo boxes
-    const bool in = interior(a, ix, iz);
-    const float tp = in ? taper_at(a, ix, iz) : 1.f;
-    const float lxx = LXX[s], lzz = LZZ[s], lxz = LXZ[s];
-    // tau-bar^n
-    a.olt[0][p] = tp * lxx;
-    a.olt[1][p] = tp * lzz;
-    a.olt[2][p] = tp * lxz;
-    // E^T (dt C y):  v-bar_x += -D-_x(p_x)/dx - D-_z(q)/dz,
-    //                v-bar_z += -D+_z(p_z)/dz - D+_x(q)/dx
-    const float dxm_px = c1 * (PX[s] - PX[s - W]) + c2 * (PX[s - 2 * W] - PX[s + W]);
-    const float dzm_q = c1 * (QQ[s] - QQ[s - 1]) + c2 * (QQ[s - 2] - QQ[s + 1]);
-    const float dzp_pz = c1 * (PZ[s + 1] - PZ[s]) + c2 * (PZ[s - 1] - PZ[s + 2]);
-    const float dxp_q = c1 * (QQ[s + W] - QQ[s]) + c2 * (QQ[s - W] - QQ[s + 2 * W]);
-    const float lvx = LVX[v], lvz = LVZ[v];
-    float ovx = tp * lvx - dxm_px * a.idx - dzm_q * a.idz;
-    float ovz = tp * lvz - dzp_pz * a.idz - dxp_q * a.idx;
-    // Receiver terms v-bar^n(rec) += adj[r][n].
-    for (int i = r0; i < r1; ++i) {
-      const int rr = a.rec_list[i];
-      if (a.rec_cell[rr] == (int)p) {
-        ovx = ovx + (float)a.adj_x[(size_t)rr * a.nt + a.it];
-        ovz = ovz + (float)a.adj_z[(size_t)rr * a.nt + a.it];
-      }
-    }
-    a.olv[0][p] = ovx;
-    a.olv[1][p] = ovz;
-    float2 g_b = gb[j];
-    if (in) {
-      // grad_b += dt T lv . A tau^{n+1}
-      const float ax = (c1 * (FXX[s] - FXX[s - W]) + c2 * (FXX[s - 2 * W] - FXX[s + W])) * a.idx +
-                       (c1 * (FXZ[s] - FXZ[s - 1]) + c2 * (FXZ[s - 2] - FXZ[s + 1])) * a.idz;
-      const float az = (c1 * (FXZ[s + W] - FXZ[s]) + c2 * (FXZ[s - W] - FXZ[s + 2 * W])) * a.idx +
-                       (c1 * (FZZ[s + 1] - FZZ[s]) + c2 * (FZZ[s - 1] - FZZ[s + 2])) * a.idz;
-      g_b = ff_add(g_b, (a.dt * tp) * (lvx * ax + lvz * az));
-      // Medium gradients from the strain rates of v^n.
-      const float ex = (c1 * (FVX[s + W] - FVX[s]) + c2 * (FVX[s - W] - FVX[s + 2 * W])) * a.idx;
-      const float ez = (c1 * (FVZ[s] - FVZ[s - 1]) + c2 * (FVZ[s - 2] - FVZ[s + 1])) * a.idz;
-      const float gxz = (c1 * (FVX[s + 1] - FVX[s]) + c2 * (FVX[s - 1] - FVX[s + 2])) * a.idz +
-                        (c1 * (FVZ[s] - FVZ[s - W]) + c2 * (FVZ[s - 2 * W] - FVZ[s + W])) * a.idx;
-      const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
-      a.g_lm[u] = ff_add(glm[j], a.dt * (yxx * ex + yzz * ez));
-      a.g_la[u] = ff_add(gla[j], a.dt * (yxx * ez + yzz * ex));
-      a.g_mu[u] = ff_add(gmu[j], a.dt * yxz * gxz);
-    }
-    // Source terms s = coef stf dt b / div at their points depend on b.
-    const InjPlan &pl = a.plan;
-    bool src = false;
-    if (pl.n && ix >= pl.x0 && ix < pl.x0 + pl.w && iz >= pl.z0 && iz < pl.z0 + pl.h) {
-      int k = pl.map[(ix - pl.x0) * pl.h + (iz - pl.z0)];
-      for (; k >= 0 && k < pl.n && pl.terms[k].cell == (int)u; ++k) {
-        const InjTerm t = pl.terms[k];
-        if (t.kind != 0) continue;
-        const double ds = ((t.coef * a.stf[(size_t)t.index * a.nt + a.it]) * a.dt_d) / t.div;
-        g_b = ff_add(g_b, (float)(ds * (double)(t.field == 0 ? lvx : lvz)));
-        src = true;
-      }
-    }
-    if (in || src) a.g_b[u] = g_b;
-  }
+  const InjPlan &pl = a.plan;
+  const int lo = max(2, a.np - 1);
+  const bool inner = X0 - 4 >= lo && Z0 - 4 >= lo &&
+                     X0 + TX + 3 <= min(a.nx - 3, a.nx - a.np) &&
+                     Z0 + TZ + 3 <= min(a.nz - 3, a.nz - a.np) &&
+                     !(pl.n && X0 < pl.x0 + pl.w && pl.x0 < X0 + TX && Z0 < pl.z0 + pl.h &&
+                       pl.z0 < Z0 + TZ);
+  if (inner)
+    tile_body<true>(a, sm, X0, Z0, glm, gla, gmu, gb);
+  else
+    tile_body<false>(a, sm, X0, Z0, glm, gla, gmu, gb);
 }
 
 }  // namespace
