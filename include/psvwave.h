@@ -171,6 +171,18 @@ int psv_get_stf(psv_model *m, double *stf);
 int psv_get_moment(psv_model *m, double *moment);
 int psv_get_taper(psv_model *m, double *taper);
 
+/* set_stf / set_moment -- no reference counterpart: the reference fixes
+ * Ricker wavelets and dip-angle tensors (src/fdModel.cpp:214-246) and its
+ * README lists the focal mechanism as not yet generalisable. They replace
+ * the source time functions [n_sources][nt], or the moment tensors
+ * [n_sources][2][2] (row-major M00 M01 M10 M11; M01 drives the (x,z)
+ * couple and M10 the (z,x) couple of src/fdModel.cpp:681-751), for every
+ * later simulation of this model, through the same injection terms. Values
+ * must be finite. A Batch keeps the sources its members had when it was
+ * built. */
+int psv_set_stf(psv_model *m, const double *stf);
+int psv_set_moment(psv_model *m, const double *moment);
+
 /* get_model_vector / set_model_vector / get_gradient_vector --
  * src/fdModel.cpp:1358-1515; vectors of length free_parameters. */
 int psv_get_model_vector(psv_model *m, double *out);

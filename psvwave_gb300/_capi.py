@@ -87,6 +87,8 @@ _SIGNATURES = {
     "psv_get_wavefields": [_vp, _dp, _dp, _dp, _dp, _dp],
     "psv_get_stf": [_vp, _dp],
     "psv_get_moment": [_vp, _dp],
+    "psv_set_stf": [_vp, _dp],
+    "psv_set_moment": [_vp, _dp],
     "psv_get_taper": [_vp, _dp],
     "psv_get_model_vector": [_vp, _dp],
     "psv_set_model_vector": [_vp, _dp],

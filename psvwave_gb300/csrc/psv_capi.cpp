@@ -376,6 +376,20 @@ int psv_get_moment(psv_model *m, double *moment) {
   });
 }
 
+int psv_set_stf(psv_model *m, const double *stf) {
+  return guarded([&] {
+    need(stf, "stf");
+    M(m).set_stf(stf);
+  });
+}
+
+int psv_set_moment(psv_model *m, const double *moment) {
+  return guarded([&] {
+    need(moment, "moment");
+    M(m).set_moment(moment);
+  });
+}
+
 int psv_get_taper(psv_model *m, double *taper) {
   return guarded([&] {
     need(taper, "taper");

@@ -1478,6 +1478,31 @@ void Model::get_wavefields(double *out[5]) {
 void Model::get_stf(double *out) const { std::copy(stf_.begin(), stf_.end(), out); }
 void Model::get_moment(double *out) const { std::copy(moment_.begin(), moment_.end(), out); }
 
+void Model::set_stf(const double *stf) {
+  DeviceGuard guard(device_);
+  for (size_t i = 0; i < stf_.size(); ++i)
+    if (!std::isfinite(stf[i])) throw Error(PSV_ERR_INVALID_ARGUMENT, "stf must be finite");
+  synchronize();  // work in flight reads the device copy
+  std::copy(stf, stf + stf_.size(), stf_.begin());
+  if (!stf_.empty())
+    cuda_check(cudaMemcpy(stf_d_.get(), stf_.data(), stf_.size() * sizeof(double),
+                          cudaMemcpyHostToDevice),
+               "upload stf");
+}
+
+void Model::set_moment(const double *moment) {
+  DeviceGuard guard(device_);
+  for (size_t i = 0; i < moment_.size(); ++i)
+    if (!std::isfinite(moment[i])) throw Error(PSV_ERR_INVALID_ARGUMENT, "moment must be finite");
+  synchronize();
+  std::copy(moment, moment + moment_.size(), moment_.begin());
+  // The injection terms carry the tensor: rebuild them, and everything that
+  // holds their device addresses (descriptors, captured pipelines).
+  clear_graphs();
+  build_plans();
+  if (tma_ok_) build_descs();
+}
+
 void Model::get_taper(double *out) const {
   const int nx = geo_.nx, nz = geo_.nz, np = cfg_.np_boundary;
   for (int ix = 0; ix < nx; ++ix)

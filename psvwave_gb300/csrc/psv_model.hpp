@@ -121,6 +121,10 @@ class Model {
   void get_wavefields(double *out[5]);
   void get_stf(double *out) const;
   void get_moment(double *out) const;
+  // Source generalisation: custom wavelets [n_sources][nt] and full 2 x 2
+  // moment tensors [n_sources][2][2] for every later simulation.
+  void set_stf(const double *stf);
+  void set_moment(const double *moment);
   void get_taper(double *out) const;
 
   void get_model_vector(double *out);

@@ -133,6 +133,9 @@ class fdModel:
     nx_free_parameters = _i("nx_free_parameters")
     nz_free_parameters = _i("nz_free_parameters")
     free_parameters = _i("free_parameters")
+    # basis block size (points per model-vector cell in x and z)
+    npx = _i("basis_gridpoints_x")
+    npz = _i("basis_gridpoints_z")
     snapshot_interval = _i("snapshot_interval")
     snapshots = _i("snapshots")
     n_shots = _i("n_shots")
@@ -341,6 +344,25 @@ class fdModel:
         out = _out((self.n_sources, 2, 2))
         _capi.check(self._lib.psv_get_moment(self._h, _ptr(out)))
         return out
+
+    def set_stf(self, stf):
+        """Custom source time functions [n_sources][nt] in place of the
+        Ricker wavelets, for every later simulation (no reference
+        counterpart: source generalisation)."""
+        a = np.ascontiguousarray(np.asarray(stf, dtype=np.float64))
+        if a.shape != (self.n_sources, self.nt):
+            raise ValueError("stf must have shape (n_sources, nt)")
+        _capi.check(self._lib.psv_set_stf(self._h, _ptr(a)))
+
+    def set_moment(self, moment):
+        """Full 2 x 2 moment tensors [n_sources][2][2] (M01 drives the (x,z)
+        couple, M10 the (z,x) couple) in place of the dip-angle tensors, for
+        every later simulation (no reference counterpart: source
+        generalisation)."""
+        a = np.ascontiguousarray(np.asarray(moment, dtype=np.float64))
+        if a.shape != (self.n_sources, 2, 2):
+            raise ValueError("moment must have shape (n_sources, 2, 2)")
+        _capi.check(self._lib.psv_set_moment(self._h, _ptr(a)))
 
     def get_taper(self):
         out = _out((self.nx, self.nz))
