@@ -45,6 +45,9 @@ def parse():
                    help="skip the FWI-gradient and batching measurements")
     p.add_argument("--ncu-case", type=int, default=0, metavar="NT",
                    help="run one NT-step forward of the c1 workload and exit (for ncu captures)")
+    p.add_argument("--ncu-case-exact", type=int, default=0, metavar="NT",
+                   help="run one exact gradient of one NT-step shot of the c3 workload, launch by "
+                        "launch, and exit (for ncu captures)")
     return p.parse_args()
 
 
@@ -356,10 +359,31 @@ def ncu_case(nt):
         m.kernel_variant, m.tile_shape, m.get_synthetic_data()[0].sum()))
 
 
+def ncu_case_exact(nt):
+    """One exact gradient (checkpoints every 100 steps) of a one-shot, NT-step
+    version of the c3 workload, kernels launched one by one (no graph), for
+    ncu captures."""
+    import psvwave_gb300 as psv
+    from psvwave_gb300 import workloads
+
+    true, start = workloads.c3_media(workloads.c3_params())
+    m = psv.fdModel.from_parameters(workloads.c3_params(nt=nt, n_shots=1))
+    m.set_parameter_fields(*true)
+    m.forward_simulate(0, False)
+    m.set_observed_data(*m.get_synthetic_data())
+    m.set_parameter_fields(*start)
+    m.set_graph_capture(False)
+    mis, _ = m.exact_gradient(100)
+    print("ncu exact case: %s tiles, misfit %.9e" % (m.tile_shape, mis))
+
+
 def main():
     args = parse()
     if args.ncu_case:
         ncu_case(args.ncu_case)
+        return
+    if args.ncu_case_exact:
+        ncu_case_exact(args.ncu_case_exact)
         return
     if args.impl == "reference":
         run_reference(args)
