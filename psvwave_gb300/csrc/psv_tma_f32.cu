@@ -124,7 +124,8 @@ __device__ __forceinline__ bool interior_tile(const SimDesc &d, int X0, int Z0, 
 template <class S, int CFG, bool ADJ>
 __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, int X0, int Z0,
                                           bool first, int tile, int it, int parity, int store,
-                                          int *err, uint32_t phase, bool init_bar) {
+                                          int *err, uint32_t phase, bool init_bar,
+                                          bool sync_copy = true) {
   constexpr int TX = S::TX, TZ = S::TZ, W = S::W, VR = S::VR, SR = S::SR, G = S::G;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>(
@@ -172,7 +173,10 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
     bb[k] = (col_ok && gx < nx) ? __ldg(d.b + gx * ps + gzc) : 0.f;
   }
   griddep_wait();
-  __syncthreads();
+  // (sync_copy false: the caller has just passed a barrier that follows
+  // every thread's last access of the tile buffers, and the mbarrier is
+  // initialised.)
+  if (sync_copy) __syncthreads();
   if (threadIdx.x == 0) {
     // Order this CTA's earlier generic accesses of the tile buffers before
     // the copies overwrite them.
@@ -470,49 +474,68 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
   const long long total = (long long)n_steps * n_tiles;
   uint32_t phase = 0;
   bool init = true;
-  // Thread 0 fetches the next item while the current one runs.
+  // Thread 0 holds the item after the current one and the finished item it
+  // has yet to publish. Per item, after the barrier that ends the previous
+  // one: thread 0 publishes that item (fence + release) while warp 1's first
+  // nine lanes poll the new item's neighbours, and one barrier lets the CTA
+  // go on. A poll may wait on this CTA's own publication, which thread 0
+  // makes without waiting on anything.
   unsigned next = 0;
-  if (threadIdx.x == 0) next = atomicAdd(sched, 1u);
+  int pub_tile = -1;
+  unsigned pub_count = 0;
+  if (threadIdx.x == 0) {
+    s_item = (int)atomicAdd(sched, 1u);
+    next = atomicAdd(sched, 1u);
+  }
+  __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) {
-      s_item = (int)next;
-      next = atomicAdd(sched, 1u);
-    }
-    __syncthreads();
     const long long w = s_item;
-    if (w >= total) return;
+    if (w >= total) {
+      if (threadIdx.x == 0 && pub_tile >= 0) {
+        __threadfence();
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + pub_tile),
+                     "r"(pub_count)
+                     : "memory");
+      }
+      return;
+    }
     const int j = (int)(w / n_tiles), tile = (int)(w - (long long)j * n_tiles);
     const int tx = tile / tiles_z, tz = tile - tx * tiles_z;
-    if (j > 0) {
-      // Nine threads wait on the tile and its eight neighbours at once.
-      bool ok = true;
-      if (threadIdx.x < 9) {
-        const int a = tx + (int)threadIdx.x / 3 - 1, b = tz + (int)threadIdx.x % 3 - 1;
-        if (a >= 0 && a < tiles_x && b >= 0 && b < tiles_z)
-          ok = wait_at_least(sched + 1 + a * tiles_z + b, (unsigned)j);
-      }
-      if (!__syncthreads_and(ok)) {
-        if (threadIdx.x == 0) atomicOr(err, 2);
-        return;
-      }
-      // The copies (async proxy) must see what the generic stores of other
-      // CTAs made visible to the waiting threads.
-      if (threadIdx.x == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
+    bool ok = true;
+    if (j > 0 && threadIdx.x >= 32 && threadIdx.x < 41) {
+      const int k = (int)threadIdx.x - 32;
+      const int a = tx + k / 3 - 1, b = tz + k % 3 - 1;
+      if (a >= 0 && a < tiles_x && b >= 0 && b < tiles_z)
+        ok = wait_at_least(sched + 1 + a * tiles_z + b, (unsigned)j);
     }
+    if (threadIdx.x == 0 && pub_tile >= 0) {
+      __threadfence();
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + pub_tile),
+                   "r"(pub_count)
+                   : "memory");
+      pub_tile = -1;
+    }
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) atomicOr(err, 2);
+      return;
+    }
+    // The copies (async proxy) must see what the generic stores of other
+    // CTAs made visible to the polling threads.
+    if (j > 0 && threadIdx.x == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
     const int it = ADJ ? it0 - j : it0 + j;
     const int parity = parity0 ^ (j & 1);
     if (!step_body<S, CFG, ADJ>(d, d.maps[parity], tx * S::TX, tz * S::TZ, false, tile, it, parity,
-                                store, err, phase, init))
+                                store, err, phase, init, init))
       return;
     phase ^= 1u;
     init = false;
-    __syncthreads();  // every thread's stores of the item are issued
     if (threadIdx.x == 0) {
-      __threadfence();
-      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + tile),
-                   "r"((unsigned)(j + 1))
-                   : "memory");
+      pub_tile = tile;
+      pub_count = (unsigned)(j + 1);
+      s_item = (int)next;
+      next = atomicAdd(sched, 1u);
     }
+    __syncthreads();  // every thread's stores of the item are issued; s_item is the next item
   }
 }
 
