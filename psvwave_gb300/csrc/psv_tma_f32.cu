@@ -465,6 +465,9 @@ __device__ __forceinline__ bool wait_at_least(const unsigned *p, unsigned v) {
 // The earliest unfinished item always has its inputs ready, so the
 // schedule cannot deadlock; each wait is bounded nonetheless, and a CTA
 // that gives up raises *err and stops (its dependents then time out too).
+// Publication is a barrier followed by one thread's st.release.gpu: release
+// is cumulative, so it orders every store of the CTA that precedes the
+// barrier, and the waiting side's ld.acquire.gpu sees them all.
 template <class S, int CFG, bool ADJ>
 __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
     fused_steps_tma(const __grid_constant__ SimDesc d, int tiles_x, int tiles_z, int it0,
@@ -492,7 +495,6 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
     const long long w = s_item;
     if (w >= total) {
       if (threadIdx.x == 0 && pub_tile >= 0) {
-        __threadfence();
         asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + pub_tile),
                      "r"(pub_count)
                      : "memory");
@@ -509,7 +511,8 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
         ok = wait_at_least(sched + 1 + a * tiles_z + b, (unsigned)j);
     }
     if (threadIdx.x == 0 && pub_tile >= 0) {
-      __threadfence();
+      // The release orders everything that precedes it in causality order:
+      // every thread's stores of the item, through the barrier that ended it.
       asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + pub_tile),
                    "r"(pub_count)
                    : "memory");
@@ -588,9 +591,8 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
       return;
     phase ^= 1u;
     init = false;
-    __syncthreads();
+    __syncthreads();  // every thread's stores of the item precede the release
     if (threadIdx.x == 0) {
-      __threadfence();
       asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + k),
                    "r"((unsigned)(j + 1))
                    : "memory");
