@@ -187,7 +187,7 @@ def fwi_gradients(steps, warmup, with_cpu):
            "workload": "c0: 250x150 grid, nt=4000, 2 sources in 1 shot, 19 receivers, "
                        "snapshot interval 10; forward + misfit + adjoint + kernels per gradient",
            "ms_per_gradient": 1e3 * dt / steps, "misfit": m.misfit,
-           "tile_shape": m.tile_shape,
+           "tile_shape": m.tile_shape, "kernel_variant": m.kernel_variant,
            "fp64": {"value": steps / dt64, "ms_per_gradient": 1e3 * dt64 / steps,
                     "misfit": m64.misfit,
                     "note": "the reference's precision, bit-identical to it"}}

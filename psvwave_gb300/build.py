@@ -32,6 +32,7 @@ UNITS = [
     ("psv_fast_f32.cu", []),
     ("psv_tma_f32.cu", []),
     ("psv_exact_tma.cu", []),
+    ("psv_cluster_f32.cu", []),
     ("psv_aux.cu", ["-fmad=false"]),
     ("psv_noalloc.cu", []),
     ("psv_config.cpp", []),

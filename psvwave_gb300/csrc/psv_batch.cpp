@@ -101,6 +101,7 @@ void Batch::build() {
     d.idz = static_cast<float>(1.0 / c.dz);
     d.dt_d = c.dt;
     d.lm = m.lm_.as<float>();
+    d.mu = m.mu_.as<float>();
     d.b = m.b_.as<float>();
     d.taper_tab = m.taper_tab_d_.as<float>();
     for (int f = 0; f < 5; ++f)

@@ -14,6 +14,7 @@
 #include <sstream>
 
 #include "../../include/psvwave.h"
+#include "psv_cluster.hpp"
 #include "psv_exact_tma.hpp"
 #include "psv_fast.hpp"
 
@@ -107,6 +108,10 @@ Model::Model(const Config &cfg, int precision, int device)
     if (tile_cfg_ == tma::kTile32x60 && slots > 0 &&
         tma::tile_count(tile_cfg_, geo_.nx, geo_.nz) >= slots)
       variant_ = kFusedTmaPersistent;
+    // Grids that one thread-block cluster holds in shared memory run
+    // cluster-resident (up to kClusterCells points).
+    if (cluster_nc_ > 0 && static_cast<double>(geo_.nx) * geo_.nz <= kClusterCells)
+      variant_ = kFusedCluster;
   }
   synchronize();
 }
@@ -405,6 +410,7 @@ void Model::build_descs() {
     d.idz = static_cast<float>(1.0 / cfg_.dz);
     d.dt_d = cfg_.dt;
     d.lm = lm_.as<float>();
+    d.mu = mu_.as<float>();
     d.b = b_.as<float>();
     d.taper_tab = taper_tab_d_.as<float>();
     for (int f = 0; f < 5; ++f)
@@ -457,6 +463,7 @@ void Model::build_descs() {
     }
   }
   descs_h_ = std::move(descs);
+  cluster_nc_ = cluster::plan(geo_.nx, geo_.nz, cfg_.np_boundary);
   tma_ok_ = true;
 }
 
@@ -474,6 +481,12 @@ cudaError_t Model::tma_forward(int shot, bool store, int it0, int it1, bool zero
   }
   const tma::SimDesc &h = descs_h_[shot];
   const int cfg = tile_cfg_;
+  if (variant_ == kFusedCluster && it1 > it0) {
+    cudaError_t e = cluster::steps(h, false, it0, it1 - it0, cur_, store, cluster_nc_, s);
+    if (e != cudaSuccess) return e;
+    cur_ ^= (it1 - it0) & 1;
+    it0 = it1;  // done; falls through to the seismograms
+  }
   if (variant_ == kFusedTmaPersistent && it1 > it0) {
     cudaError_t e = cudaMemsetAsync(sched_.get(), 0, sched_.bytes(), s);
     if (e == cudaSuccess)
@@ -513,6 +526,12 @@ cudaError_t Model::tma_adjoint(int shot) {
   cur_ = 0;
   const tma::SimDesc &h = descs_h_[cfg_.n_shots + shot];
   const int cfg = tile_cfg_;
+  if (variant_ == kFusedCluster) {
+    cudaError_t e = cluster::steps(h, true, cfg_.nt - 1, cfg_.nt, 0, false, cluster_nc_, s);
+    if (e != cudaSuccess) return e;
+    cur_ = cfg_.nt & 1;
+    return cudaGetLastError();
+  }
   if (variant_ == kFusedTmaPersistent) {
     cudaError_t e = cudaMemsetAsync(sched_.get(), 0, sched_.bytes(), s);
     if (e == cudaSuccess)
@@ -892,8 +911,11 @@ int Model::autotune(int n_steps) {
   float best = 0;
   int best_cfg = tile_cfg_, best_variant = variant_;
   bool first = true;
-  for (int v : {static_cast<int>(kFusedTma), static_cast<int>(kFusedTmaPersistent)}) {
+  std::vector<int> variants = {kFusedTma, kFusedTmaPersistent};
+  if (cluster_nc_ > 0) variants.push_back(kFusedCluster);
+  for (int v : variants) {
     for (int c = 0; c < tma::kNumTileCfgs; ++c) {
+      if (v == kFusedCluster && c > 0) break;  // no tiles: timed once
       set_variant(v);
       set_tile_cfg(c);
       forward_simulate(0, false, false, false, n_steps);  // eager
@@ -1124,7 +1146,7 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
   void *second[5] = {fields2_[0].get(), fields2_[1].get(), fields2_[2].get(), fields2_[3].get(),
                      fields2_[4].get()};
   cudaError_t err;
-  if (variant_ == kFusedTmaPersistent) {
+  if (variant_ == kFusedTmaPersistent || variant_ == kFusedCluster) {
     // One launch for all steps: time it whole; the per-step figure is its
     // share.
     cudaEventRecord(ev.front(), stream());
@@ -1174,12 +1196,16 @@ int Model::profile_forward(int shot, int n_steps, double *per_step_ms, double *k
 }
 
 void Model::set_variant(int v) {
-  if (v != kFused && v != kTwoKernel && v != kFusedTma && v != kFusedTmaPersistent)
+  if (v != kFused && v != kTwoKernel && v != kFusedTma && v != kFusedTmaPersistent &&
+      v != kFusedCluster)
     throw Error(PSV_ERR_INVALID_ARGUMENT, "unknown kernel variant");
   if (prec_ == PSV_FP64 && v != kTwoKernel)
     throw Error(PSV_ERR_INVALID_ARGUMENT, "the fused variants are FP32 only");
-  if ((v == kFusedTma || v == kFusedTmaPersistent) && !tma_ok_)
+  if ((v == kFusedTma || v == kFusedTmaPersistent || v == kFusedCluster) && !tma_ok_)
     throw Error(PSV_ERR_INVALID_ARGUMENT, "the TMA variant needs driver tensor-map support");
+  if (v == kFusedCluster && cluster_nc_ == 0)
+    throw Error(PSV_ERR_INVALID_ARGUMENT,
+                "the grid does not fit in the shared memory of one thread-block cluster");
   DeviceGuard guard(device_);
   if ((v == kTwoKernel) != (variant_ == kTwoKernel) && cur_ == 1) {
     // Bring the current state back into the primary buffers.
@@ -1198,6 +1224,7 @@ const char *Model::step_kernel_name(int k) const {
   if (variant_ == kFused) return k == 0 ? "fused_step" : "";
   if (variant_ == kFusedTma) return k == 0 ? "fused_step_tma" : "";
   if (variant_ == kFusedTmaPersistent) return k == 0 ? "fused_steps_tma" : "";
+  if (variant_ == kFusedCluster) return k == 0 ? "cluster_steps" : "";
   return k == 0 ? "stress_step" : (k == 1 ? "velocity_step" : "");
 }
 

@@ -164,7 +164,11 @@ class Model {
   size_t exact_bytes(int checkpoint_every) const;
   int variant() const { return variant_; }
   int kernels_per_step() const { return variant_ == kTwoKernel ? 2 : 1; }
-  bool is_tma() const { return variant_ == kFusedTma || variant_ == kFusedTmaPersistent; }
+  // The FP32 variants built on the TMA step's descriptors (the cluster
+  // variant shares them, and the exact adjoint's recompute runs the TMA step).
+  bool is_tma() const {
+    return variant_ == kFusedTma || variant_ == kFusedTmaPersistent || variant_ == kFusedCluster;
+  }
   const char *step_kernel_name(int k) const;
 
   void set_stream(cudaStream_t s) { user_stream_ = s; }
@@ -211,6 +215,8 @@ class Model {
 
   int pitch_ = 0;
   int variant_ = kTwoKernel;
+  int cluster_nc_ = 0;  // CTAs of the cluster that holds the grid, 0 if none does
+  static constexpr double kClusterCells = 1.0e5;  // default cluster-resident up to this size
   int cur_ = 0;  // fused variants: 0 = fields_ hold the current state, 1 = fields2_
   // TMA step: one simulation descriptor per (direction, shot) --
   // [0, n_shots) forward, [n_shots, 2 n_shots) adjoint -- on the host (their

@@ -73,7 +73,13 @@ struct SolverArgs {
 // (both precisions; the FP64 path always uses it). kFused: one fused_step
 // launch per time step over ping-pong buffers (FP32). kFusedTma: the same
 // step with TMA tile loads (FP32, nz % 4 == 0; the default where it applies).
-enum Variant { kFused = 0, kTwoKernel = 1, kFusedTma = 2, kFusedTmaPersistent = 3 };
+enum Variant {
+  kFused = 0,
+  kTwoKernel = 1,
+  kFusedTma = 2,
+  kFusedTmaPersistent = 3,
+  kFusedCluster = 4
+};
 
 // Precision-specific entry points (defined in psv_solver_f32.cu / _f64.cu).
 #define PSV_SOLVER_DECLS(SUFFIX)                                                          \

@@ -36,6 +36,7 @@ struct alignas(128) SimDesc {
   float dt = 0, idx = 0, idz = 0;
   double dt_d = 0;
   const float *lm = nullptr, *b = nullptr, *taper_tab = nullptr;
+  const float *mu = nullptr;  // (the TMA steps read mu through the maps)
   float *accu[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // this shot's snapshots
   double *krho = nullptr, *klam = nullptr, *kmu = nullptr;
   double sidt = 0;

@@ -32,6 +32,7 @@
 
 #include "psv_tma.hpp"
 #include "psv_tma_ptx.cuh"
+#include "psv_tma_terms.cuh"
 
 namespace psv {
 namespace tma {
@@ -60,46 +61,6 @@ struct Shape {
 };
 using Big = Shape<32, 60, 256>;
 using Small = Shape<16, 28, 128>;
-
-__device__ __forceinline__ void correlate(const SimDesc &d, const float *const asnap[5], int g,
-                                          float lm, float mu, float vx, float vz, float txx,
-                                          float tzz, float txz) {
-  const float la = lm - 2.0f * mu;
-  const float avx = asnap[0][g], avz = asnap[1][g], atxx = asnap[2][g], atzz = asnap[3][g],
-              atxz = asnap[4][g];
-  const float r = la / lm;
-  const float dd = lm - la * r;
-  const float inv_den = 1.0f / (dd * dd);
-  const float fxx = txx - tzz * r, fzz = tzz - txx * r;
-  const float axx = atxx - atzz * r, azz = atzz - atxx * r;
-  const float lam = (axx + azz) * (fxx + fzz) * inv_den;
-  const float muk = (fxx * axx + fzz * azz) * inv_den + 2.0f * (txz * atxz / (4.0f * mu * mu));
-  d.krho[g] -= d.sidt * static_cast<double>(avx * vx + avz * vz);
-  d.klam[g] += d.sidt * static_cast<double>(lam);
-  d.kmu[g] += d.sidt * 2.0 * static_cast<double>(muk);
-}
-
-__device__ __forceinline__ void inject(const SimDesc &d, int it, int g, int gx, int gz, float b,
-                                       float &vx, float &vz) {
-  const InjPlan &p = d.plan;
-  int k = p.map[(gx - p.x0) * p.h + (gz - p.z0)];
-  if (k < 0) return;
-  for (; k < p.n && p.terms[k].cell == g; ++k) {
-    const InjTerm t = p.terms[k];
-    double term;
-    if (t.kind == 0) {
-      term = (((t.coef * d.stf[(size_t)t.index * d.nt + it]) * d.dt_d) * (double)b) / t.div;
-    } else {
-      const double *src = t.field == 0 ? d.a_ux : d.a_uz;
-      term = ((d.dt_d * (double)b) * src[(size_t)t.index * d.nt + it]) / t.div;
-    }
-    if (t.field == 0)
-      vx += (float)term;
-    else
-      vz += (float)term;
-  }
-}
-
 
 // An interior tile computes every stress point of its box (rows X0-2 ..
 // X0+TX+1, columns Z0-2 .. Z0+TZ+1) inside the updated region 2 <= x < n-2
@@ -556,47 +517,65 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
   const long long total = (long long)n_steps * n_tiles;
   uint32_t phase = 0;
   bool init = true;
+  // As fused_steps_tma: thread 0 publishes the finished item while warp 1
+  // polls the new item's neighbours.
   unsigned next = 0;
-  if (threadIdx.x == 0) next = atomicAdd(sched, 1u);
+  int pub = -1;
+  unsigned pub_count = 0;
+  if (threadIdx.x == 0) {
+    s_item = (int)atomicAdd(sched, 1u);
+    next = atomicAdd(sched, 1u);
+  }
+  __syncthreads();
   for (;;) {
+    const long long w = s_item;
+    if (w >= total) {
+      if (threadIdx.x == 0 && pub >= 0)
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + pub),
+                     "r"(pub_count)
+                     : "memory");
+      return;
+    }
+    const int j = (int)(w / n_tiles), k = (int)(w - (long long)j * n_tiles);
+    const int4 t = tiles[k];
+    const bool skip = active && !active[t.x];  // uniform: t is the CTA's
+    const SimDesc &d = sims[t.x];
+    const int tx = t.y / S::TX, tz = t.z / S::TZ;
+    bool ok = true;
+    if (!skip && j > 0 && threadIdx.x >= 32 && threadIdx.x < 41) {
+      const int q = (int)threadIdx.x - 32;
+      const int a = tx + q / 3 - 1, b = tz + q % 3 - 1;
+      if (a >= 0 && a < d.tiles_x && b >= 0 && b < d.tiles_z)
+        ok = wait_at_least(sched + 1 + d.tile_base + a * d.tiles_z + b, (unsigned)j);
+    }
+    if (threadIdx.x == 0 && pub >= 0) {
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + pub),
+                   "r"(pub_count)
+                   : "memory");
+      pub = -1;
+    }
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) atomicOr(err, 2);
+      return;
+    }
+    if (!skip) {
+      if (j > 0 && threadIdx.x == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
+      const int parity = j & 1;
+      if (!step_body<S, CFG, false>(d, d.maps[parity], t.y, t.z, false, tx * d.tiles_z + tz, j,
+                                    parity, store, err, phase, init, init))
+        return;
+      phase ^= 1u;
+      init = false;
+      if (threadIdx.x == 0) {
+        pub = k;
+        pub_count = (unsigned)(j + 1);
+      }
+    }
     if (threadIdx.x == 0) {
       s_item = (int)next;
       next = atomicAdd(sched, 1u);
     }
-    __syncthreads();
-    const long long w = s_item;
-    __syncthreads();  // everyone has read s_item before thread 0 rewrites it
-    if (w >= total) return;
-    const int j = (int)(w / n_tiles), k = (int)(w - (long long)j * n_tiles);
-    const int4 t = tiles[k];
-    if (active && !active[t.x]) continue;  // uniform: t is the CTA's
-    const SimDesc &d = sims[t.x];
-    const int tx = t.y / S::TX, tz = t.z / S::TZ;
-    if (j > 0) {
-      bool ok = true;
-      if (threadIdx.x < 9) {
-        const int a = tx + (int)threadIdx.x / 3 - 1, b = tz + (int)threadIdx.x % 3 - 1;
-        if (a >= 0 && a < d.tiles_x && b >= 0 && b < d.tiles_z)
-          ok = wait_at_least(sched + 1 + d.tile_base + a * d.tiles_z + b, (unsigned)j);
-      }
-      if (!__syncthreads_and(ok)) {
-        if (threadIdx.x == 0) atomicOr(err, 2);
-        return;
-      }
-      if (threadIdx.x == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
-    }
-    const int parity = j & 1;
-    if (!step_body<S, CFG, false>(d, d.maps[parity], t.y, t.z, false, tx * d.tiles_z + tz, j,
-                                  parity, store, err, phase, init))
-      return;
-    phase ^= 1u;
-    init = false;
-    __syncthreads();  // every thread's stores of the item precede the release
-    if (threadIdx.x == 0) {
-      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + k),
-                   "r"((unsigned)(j + 1))
-                   : "memory");
-    }
+    __syncthreads();  // the item's stores are issued; s_item is the next item
   }
 }
 

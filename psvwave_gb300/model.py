@@ -515,17 +515,21 @@ class fdModel:
         names = [self._lib.psv_step_kernel_name(self._h, k).decode() for k in range(n.value)]
         return per_step.value, dict(zip(names, list(ks)[:n.value]))
 
-    VARIANTS = {"fused": 0, "two_kernel": 1, "fused_tma": 2, "fused_tma_persistent": 3}
+    VARIANTS = {"fused": 0, "two_kernel": 1, "fused_tma": 2, "fused_tma_persistent": 3,
+                "fused_cluster": 4}
 
     @property
     def kernel_variant(self):
-        """'fused_tma' (one launch per step with TMA tile loads; the FP32
-        default), 'fused_tma_persistent' (the same step, all time steps in
-        one persistent launch), 'fused' (one launch per step, FP32) or
-        'two_kernel' (stress and velocity launches; the FP64 variant)."""
+        """'fused_tma' (one launch per step with TMA tile loads),
+        'fused_tma_persistent' (the same step, all time steps in one
+        persistent launch; the default on large grids), 'fused_cluster'
+        (all time steps in one launch of one thread-block cluster holding
+        the grid in shared memory; the default on small grids), 'fused' (one
+        launch per step, FP32) or 'two_kernel' (stress and velocity
+        launches; the FP64 variant)."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_get_kernel_variant(self._h, ctypes.byref(v)))
-        return {0: "fused", 1: "two_kernel", 2: "fused_tma", 3: "fused_tma_persistent"}[v.value]
+        return {k: n for n, k in self.VARIANTS.items()}[v.value]
 
     @kernel_variant.setter
     def kernel_variant(self, name):

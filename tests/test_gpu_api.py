@@ -243,4 +243,4 @@ def test_large_grid_defaults_to_persistent_launch():
     assert m.tile_shape == "32x60"
     assert m.kernel_variant == "fused_tma_persistent"
     small = psv.fdModel(SMALL_INI)
-    assert small.kernel_variant == "fused_tma"
+    assert small.kernel_variant == "fused_cluster"

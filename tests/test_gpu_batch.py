@@ -26,6 +26,7 @@ def test_batch_matches_individual_runs(shape, persistent):
     models = small_models()
     ref = []
     for m in models:
+        m.kernel_variant = "fused_tma"  # the batch's step kernel
         m.tile_shape = shape
         out = []
         for s in range(m.n_shots):

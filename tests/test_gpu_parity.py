@@ -156,16 +156,23 @@ def test_fp32_vs_fp64_gpu_nb2_full_outputs():
 
 
 def test_default_variants():
-    """FP32 models use the TMA step whatever nz is (rows are padded to 16
-    bytes: nz = 56 and nz = 150 alike); FP64 models the two-kernel step."""
-    assert psv.fdModel(SMALL_INI).kernel_variant == "fused_tma"   # nz = 56
-    assert psv.fdModel(NB2_INI).kernel_variant == "fused_tma"     # nz = 150, padded to 152
+    """Small FP32 grids run cluster-resident, whatever nz is (nz = 56 and
+    nz = 150, padded to 152); the TMA step is available on them too; FP64
+    models use the two-kernel step."""
+    for ini in (SMALL_INI, NB2_INI):
+        m = psv.fdModel(ini)
+        assert m.kernel_variant == "fused_cluster"
+        m.kernel_variant = "fused_tma"
+        assert m.kernel_variant == "fused_tma"
     assert psv.fdModel(SMALL_INI, precision="fp64").kernel_variant == "two_kernel"
     with pytest.raises(ValueError):
         psv.fdModel(SMALL_INI, precision="fp64").kernel_variant = "fused_tma"
+    with pytest.raises(ValueError):
+        psv.fdModel(SMALL_INI, precision="fp64").kernel_variant = "fused_cluster"
 
 
-@pytest.mark.parametrize("variant", ["fused_tma", "fused_tma_persistent", "fused", "two_kernel"])
+@pytest.mark.parametrize("variant", ["fused_cluster", "fused_tma", "fused_tma_persistent", "fused",
+                                     "two_kernel"])
 def test_fp32_variants_within_tolerance(golden, variant):
     m = psv.fdModel(SMALL_INI, precision="fp32")
     m.kernel_variant = variant
@@ -271,3 +278,47 @@ def test_persistent_step_matches_per_step_launches_bitwise(golden, shape, ini):
     assert m0 == m1
     for a, b in zip(d0 + s0 + k0, d1 + s1 + k1):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("ini", [SMALL_INI, NB2_INI])
+def test_cluster_matches_per_step_launches_bitwise(golden, ini):
+    """The cluster-resident variant keeps the grid in the shared memory of
+    one thread-block cluster and runs the point arithmetic of the TMA step's
+    general path. On the small grid every TMA tile takes that path, and
+    forward seismograms and snapshots, the adjoint's kernels, the misfit and
+    the final wave fields are identical bit for bit. On the Notebook 2 grid
+    interior TMA tiles take their fast path (no taper factor, so the
+    compiler contracts a few products differently) and everything agrees to
+    FP32 rounding."""
+    res = []
+    for variant in ("fused_tma", "fused_cluster"):
+        m = psv.fdModel(ini, precision="fp32")
+        m.kernel_variant = variant
+        if ini == SMALL_INI:
+            target, start = tuple(golden["target"]), tuple(golden["start"])
+        else:
+            target, start = nb2_media(m.nx, m.nz, m.np_boundary, m.dx, m.dz)
+        m.set_parameter_fields(*target)
+        for s in range(m.n_shots):
+            m.forward_simulate(s, False)
+        m.set_observed_data(*m.get_synthetic_data())
+        m.set_parameter_fields(*start)
+        for s in range(m.n_shots):
+            m.forward_simulate(s, True)
+        fwd = m.get_wavefields()
+        m.calculate_l2_misfit()
+        m.calculate_l2_adjoint_sources()
+        m.reset_kernels()
+        for s in range(m.n_shots):
+            m.adjoint_simulate(s)
+        res.append((m.get_synthetic_data(), m.get_snapshots(), m.get_lame_kernels(), fwd,
+                    m.get_wavefields(), m.misfit))
+    (d0, s0, k0, f0, a0, m0), (d1, s1, k1, f1, a1, m1) = res
+    if ini == SMALL_INI:
+        assert m0 == m1
+        for a, b in zip(d0 + s0 + k0 + f0 + a0, d1 + s1 + k1 + f1 + a1):
+            assert np.array_equal(a, b)
+    else:
+        assert abs(m0 - m1) <= 1e-6 * abs(m0)
+        for a, b in zip(d0 + s0 + k0, d1 + s1 + k1):
+            assert rel_l2(a, b) <= 1e-5
