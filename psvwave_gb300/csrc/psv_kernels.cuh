@@ -294,6 +294,17 @@ __global__ void narrow_kernel(size_t n, const double *src, T *dst) {
 
 // ------------------------------------------------------------- drivers --
 
+namespace kern {
+// Rows of the two-kernel step's 32-column CTAs. FP64 keeps the FP64 pipe
+// busy on every SM it has work on, so small CTAs (2 rows) spread the grid
+// evenly over the SMs: at 250 x 150, 32 x 8 CTAs made 160 CTAs for 152 SMs
+// and eight SMs ran two, doubling the step; 32 x 2 CTAs make 625.
+template <typename T>
+struct BlockRows {
+  static constexpr int value = sizeof(T) == 8 ? 2 : 8;
+};
+}  // namespace kern
+
 template <typename T>
 kern::Grid<T> make_grid(const SolverArgs &a) {
   kern::Grid<T> g;
@@ -336,8 +347,8 @@ cudaError_t run_forward(const SolverArgs &a, const InjPlan &plan, int shot, bool
     if (err != cudaSuccess) return err;
   }
   const kern::Grid<T> g = make_grid<T>(a);
-  const dim3 block(32, 8);
-  const dim3 grid((a.nz + 31) / 32, (a.nx + 7) / 8);
+  const dim3 block(32, kern::BlockRows<T>::value);
+  const dim3 grid((a.nz + 31) / 32, (a.nx + block.y - 1) / block.y);
   const size_t gsz = (size_t)a.nx * a.nz;
   T *raw = (T *)a.rec_raw;
   kern::StressExtras<T, false> e{};
@@ -385,8 +396,8 @@ cudaError_t run_adjoint(const SolverArgs &a, const InjPlan &plan, int shot, cuda
   cudaError_t err = zero_fields<T>(a, s);
   if (err != cudaSuccess) return err;
   const kern::Grid<T> g = make_grid<T>(a);
-  const dim3 block(32, 8);
-  const dim3 grid((a.nz + 31) / 32, (a.nx + 7) / 8);
+  const dim3 block(32, kern::BlockRows<T>::value);
+  const dim3 grid((a.nz + 31) / 32, (a.nx + block.y - 1) / block.y);
   const size_t gsz = (size_t)a.nx * a.nz;
   kern::StressExtras<T, true> e{};
   e.krho = a.k_rho;
