@@ -264,13 +264,14 @@ enum psv_variant {
 int psv_set_kernel_variant(psv_model *m, int variant);
 int psv_get_kernel_variant(const psv_model *m, int *variant);
 
-/* Tile shape of the FP32 TMA step: PSV_TILE_32X60 (x rows by z columns;
- * large grids) or PSV_TILE_16X28 (small grids; chosen by default below
- * 400,000 grid points). psv_autotune times every tile shape with both TMA
+/* Tile shape of the FP32 TMA step (x rows by z columns): PSV_TILE_32X60
+ * (256 threads; large grids), PSV_TILE_16X28 or PSV_TILE_20X28 (128
+ * threads). By default, grids with less than one wave of 32 x 60 tiles take
+ * 16 x 28. psv_autotune times every tile shape with both TMA
  * launch schemes (PSV_VARIANT_FUSED_TMA and _PERSISTENT) on n_steps forward
  * steps of shot 0, replayed as CUDA graphs, keeps the fastest pair and
  * returns its shape in *chosen. No counterpart in the reference. */
-enum psv_tile_shape { PSV_TILE_32X60 = 0, PSV_TILE_16X28 = 1 };
+enum psv_tile_shape { PSV_TILE_32X60 = 0, PSV_TILE_16X28 = 1, PSV_TILE_20X28 = 2 };
 int psv_set_tile_shape(psv_model *m, int shape);
 int psv_get_tile_shape(const psv_model *m, int *shape);
 int psv_autotune(psv_model *m, int n_steps, int *chosen);

@@ -89,11 +89,13 @@ Model::Model(const Config &cfg, int precision, int device)
   }
   update_from_velocity();
   build_plans();
-  // Grids with at least a full wave of 32 x 60 tiles keep them; smaller ones
-  // fill the GPU with 16 x 28 tiles (at 1100 x 500, 315 large tiles against
-  // 456 resident: 12.1 us per step, 1242 small ones: 8.9 us).
-  {
-    const int big_slots = prec_ == PSV_FP32 ? tma::resident_ctas(tma::kTile32x60, false) : 0;
+  // Tile shape. Grids with at least a full wave of 32 x 60 tiles keep them
+  // (and run persistent, below); smaller ones take 16 x 28 tiles. At
+  // 1100 x 500: 32 x 60 tiles (315, against 456 resident) 12.0 us per step,
+  // 16 x 28 (1242) 8.9 us, 20 x 28 (990, one wave of 1216 resident) 9.3 us.
+  // autotune() times every shape.
+  if (prec_ == PSV_FP32) {
+    const int big_slots = tma::resident_ctas(tma::kTile32x60, false);
     if (big_slots > 0 ? tma::tile_count(tma::kTile32x60, geo_.nx, geo_.nz) < big_slots
                       : static_cast<double>(geo_.nx) * geo_.nz < 4.0e5)
       tile_cfg_ = tma::kTile16x28;
@@ -468,7 +470,7 @@ void Model::build_descs() {
 }
 
 cudaError_t Model::tma_forward(int shot, bool store, int it0, int it1, bool zero, bool finish,
-                               cudaEvent_t *events) {
+                               cudaEvent_t *events, bool allow_cluster) {
   cudaStream_t s = stream();
   if (zero) {
     const size_t bytes = padded_size() * sizeof(float);
@@ -481,7 +483,7 @@ cudaError_t Model::tma_forward(int shot, bool store, int it0, int it1, bool zero
   }
   const tma::SimDesc &h = descs_h_[shot];
   const int cfg = tile_cfg_;
-  if (variant_ == kFusedCluster && it1 > it0) {
+  if (variant_ == kFusedCluster && allow_cluster && it1 > it0) {
     cudaError_t e = cluster::steps(h, false, it0, it1 - it0, cur_, store, cluster_nc_, s);
     if (e != cudaSuccess) return e;
     cur_ ^= (it1 - it0) & 1;
@@ -673,13 +675,17 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
       // Checkpoint pass; its last segment writes its states into the slots
       // directly, and the reverse pass starts from them.
       const int last0 = (n_ck - 1) * C;
-      if (last0 > 0) cuda_check(tma_forward(shot, false, 0, 0, true, false, nullptr), "zero");
+      // The checkpoint pass runs the TMA step, as the recompute does, so that
+      // every state is the same whatever the checkpoint interval (the
+      // cluster scheme agrees with it to FP32 rounding, not bit for bit).
+      if (last0 > 0)
+        cuda_check(tma_forward(shot, false, 0, 0, true, false, nullptr, false), "zero");
       for (int k = 0; k + 1 < n_ck; ++k) {
         void *src[5], *dst[5];
         for (int f = 0; f < 5; ++f) src[f] = (cur_ ? fields2_ : fields_)[f].get();
         state(ck + k * state_bytes, dst);
         copy(src, dst, nullptr);
-        cuda_check(tma_forward(shot, false, k * C, (k + 1) * C, false, false, nullptr),
+        cuda_check(tma_forward(shot, false, k * C, (k + 1) * C, false, false, nullptr, false),
                    "exact forward");
       }
       if (last0 > 0) {

@@ -226,7 +226,8 @@ class Model {
   std::vector<tma::SimDesc> descs_h_;
   void build_descs();
   cudaError_t tma_forward(int shot, bool store, int it0, int it1, bool zero, bool finish,
-                          cudaEvent_t *events);
+                          cudaEvent_t *events,
+                          bool allow_cluster = true);
   cudaError_t tma_adjoint(int shot);
   void check_device_error();
 

@@ -61,6 +61,20 @@ struct Shape {
 };
 using Big = Shape<32, 60, 256>;
 using Small = Shape<16, 28, 128>;
+using Mid = Shape<20, 28, 128>;
+
+// Calls f with the shape type and its TileCfg value for `cfg`.
+template <class S_, int CFG_>
+struct ShapeTag {
+  using S = S_;
+  static constexpr int CFG = CFG_;
+};
+template <class F>
+decltype(auto) with_shape(int cfg, F &&f) {
+  if (cfg == kTile16x28) return f(ShapeTag<Small, kTile16x28>{});
+  if (cfg == kTile20x28) return f(ShapeTag<Mid, kTile20x28>{});
+  return f(ShapeTag<Big, kTile32x60>{});
+}
 
 // An interior tile computes every stress point of its box (rows X0-2 ..
 // X0+TX+1, columns Z0-2 .. Z0+TZ+1) inside the updated region 2 <= x < n-2
@@ -730,8 +744,12 @@ bool encode_planes(CUtensorMap *m, const float *base, int planes, size_t plane_b
 }
 
 void tile_dims(int cfg, int *tx, int *tz) {
-  *tx = cfg == kTile16x28 ? Small::TX : Big::TX;
-  *tz = cfg == kTile16x28 ? Small::TZ : Big::TZ;
+  with_shape(cfg, [&](auto t) {
+    using S = typename decltype(t)::S;
+    *tx = S::TX;
+    *tz = S::TZ;
+    return 0;
+  });
 }
 
 bool supported(int nx, int nz, int pitch) {
@@ -740,9 +758,10 @@ bool supported(int nx, int nz, int pitch) {
 
 bool make_maps(SimDesc &d, const float *mu, int cfg) {
   for (int p = 0; p < 2; ++p) {
-    const bool ok = cfg == kTile16x28
-                        ? encode_set<Small>(d.maps[p], d.set[p], d.lm, mu, d.nx, d.nz, d.pitch)
-                        : encode_set<Big>(d.maps[p], d.set[p], d.lm, mu, d.nx, d.nz, d.pitch);
+    const bool ok = with_shape(cfg, [&](auto t) {
+      using S = typename decltype(t)::S;
+      return encode_set<S>(d.maps[p], d.set[p], d.lm, mu, d.nx, d.nz, d.pitch);
+    });
     if (!ok) return false;
   }
   return true;
@@ -750,8 +769,10 @@ bool make_maps(SimDesc &d, const float *mu, int cfg) {
 
 bool encode_input_maps(Maps &m, const fast::Fields &in, const float *lm, const float *mu, int nx,
                        int nz, int pitch, int cfg) {
-  return cfg == kTile16x28 ? encode_set<Small>(m, in, lm, mu, nx, nz, pitch)
-                           : encode_set<Big>(m, in, lm, mu, nx, nz, pitch);
+  return with_shape(cfg, [&](auto t) {
+    using S = typename decltype(t)::S;
+    return encode_set<S>(m, in, lm, mu, nx, nz, pitch);
+  });
 }
 
 void append_tiles(int cfg, int sim, int nx, int nz, std::vector<int4> &tiles) {
@@ -768,11 +789,12 @@ void append_tiles(int cfg, int sim, int nx, int nz, std::vector<int4> &tiles) {
 cudaError_t step_single(const SimDesc &d, int cfg, bool adjoint, int it, int parity, bool store,
                         int *err, cudaStream_t s) {
   const int st = store ? 1 : 0;
-  if (cfg == kTile16x28)
-    return adjoint ? launch_single<Small, kTile16x28, true>(d, it, parity, st, err, s)
-                   : launch_single<Small, kTile16x28, false>(d, it, parity, st, err, s);
-  return adjoint ? launch_single<Big, kTile32x60, true>(d, it, parity, st, err, s)
-                 : launch_single<Big, kTile32x60, false>(d, it, parity, st, err, s);
+  return with_shape(cfg, [&](auto t) {
+    using S = typename decltype(t)::S;
+    constexpr int CFG = decltype(t)::CFG;
+    return adjoint ? launch_single<S, CFG, true>(d, it, parity, st, err, s)
+                   : launch_single<S, CFG, false>(d, it, parity, st, err, s);
+  });
 }
 
 int tile_count(int cfg, int nx, int nz) {
@@ -843,43 +865,42 @@ cudaError_t steps_persistent_batch(const SimDesc *sims, const int4 *tiles, int n
                                    const int *active, int cfg, int n_steps, bool store, int *err,
                                    unsigned *sched, cudaStream_t s) {
   const int st = store ? 1 : 0;
-  if (cfg == kTile16x28)
-    return launch_persistent_batch<Small, kTile16x28>(sims, tiles, n_tiles, active, n_steps, st,
-                                                      err, sched, s);
-  return launch_persistent_batch<Big, kTile32x60>(sims, tiles, n_tiles, active, n_steps, st, err,
-                                                  sched, s);
+  return with_shape(cfg, [&](auto t) {
+    using S = typename decltype(t)::S;
+    constexpr int CFG = decltype(t)::CFG;
+    return launch_persistent_batch<S, CFG>(sims, tiles, n_tiles, active, n_steps, st, err, sched,
+                                           s);
+  });
 }
 
 int resident_ctas(int cfg, bool adjoint) {
-  if (cfg == kTile16x28)
-    return adjoint ? resident<Small, kTile16x28, true>() : resident<Small, kTile16x28, false>();
-  return adjoint ? resident<Big, kTile32x60, true>() : resident<Big, kTile32x60, false>();
+  return with_shape(cfg, [&](auto t) {
+    using S = typename decltype(t)::S;
+    constexpr int CFG = decltype(t)::CFG;
+    return adjoint ? resident<S, CFG, true>() : resident<S, CFG, false>();
+  });
 }
 
 cudaError_t steps_persistent(const SimDesc &d, int cfg, bool adjoint, int it0, int n_steps,
                              int parity0, bool store, int *err, unsigned *sched, cudaStream_t s) {
   const int st = store ? 1 : 0;
-  if (cfg == kTile16x28)
-    return adjoint ? launch_persistent<Small, kTile16x28, true>(d, it0, n_steps, parity0, st, err,
-                                                                sched, s)
-                   : launch_persistent<Small, kTile16x28, false>(d, it0, n_steps, parity0, st,
-                                                                 err, sched, s);
-  return adjoint ? launch_persistent<Big, kTile32x60, true>(d, it0, n_steps, parity0, st, err,
-                                                            sched, s)
-                 : launch_persistent<Big, kTile32x60, false>(d, it0, n_steps, parity0, st, err,
-                                                             sched, s);
+  return with_shape(cfg, [&](auto t) {
+    using S = typename decltype(t)::S;
+    constexpr int CFG = decltype(t)::CFG;
+    return adjoint ? launch_persistent<S, CFG, true>(d, it0, n_steps, parity0, st, err, sched, s)
+                   : launch_persistent<S, CFG, false>(d, it0, n_steps, parity0, st, err, sched, s);
+  });
 }
 
 cudaError_t step(const SimDesc *sims, const int4 *tiles, int n_tiles, const int *active, int cfg,
                  bool adjoint, int it, int parity, bool store, int *err, cudaStream_t s) {
   const int st = store ? 1 : 0;
-  const int *a = active;
-  if (cfg == kTile16x28)
-    return adjoint ? launch<Small, kTile16x28, true>(sims, tiles, n_tiles, a, it, parity, st, err, s)
-                   : launch<Small, kTile16x28, false>(sims, tiles, n_tiles, a, it, parity, st, err,
-                                                      s);
-  return adjoint ? launch<Big, kTile32x60, true>(sims, tiles, n_tiles, a, it, parity, st, err, s)
-                 : launch<Big, kTile32x60, false>(sims, tiles, n_tiles, a, it, parity, st, err, s);
+  return with_shape(cfg, [&](auto t) {
+    using S = typename decltype(t)::S;
+    constexpr int CFG = decltype(t)::CFG;
+    return adjoint ? launch<S, CFG, true>(sims, tiles, n_tiles, active, it, parity, st, err, s)
+                   : launch<S, CFG, false>(sims, tiles, n_tiles, active, it, parity, st, err, s);
+  });
 }
 
 }  // namespace tma

@@ -535,14 +535,14 @@ class fdModel:
     def kernel_variant(self, name):
         _capi.check(self._lib.psv_set_kernel_variant(self._h, self.VARIANTS[name]))
 
-    TILE_SHAPES = {"32x60": 0, "16x28": 1}
+    TILE_SHAPES = {"32x60": 0, "16x28": 1, "20x28": 2}
 
     @property
     def tile_shape(self):
         """Tile shape (x rows by z columns) of the FP32 TMA step."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_get_tile_shape(self._h, ctypes.byref(v)))
-        return {0: "32x60", 1: "16x28"}[v.value]
+        return {k: n for n, k in self.TILE_SHAPES.items()}[v.value]
 
     @tile_shape.setter
     def tile_shape(self, name):
@@ -554,4 +554,4 @@ class fdModel:
         fastest pair and return its tile shape."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_autotune(self._h, int(n_steps), ctypes.byref(v)))
-        return {0: "32x60", 1: "16x28"}[v.value]
+        return {k: n for n, k in self.TILE_SHAPES.items()}[v.value]

@@ -244,3 +244,13 @@ def test_large_grid_defaults_to_persistent_launch():
     assert m.kernel_variant == "fused_tma_persistent"
     small = psv.fdModel(SMALL_INI)
     assert small.kernel_variant == "fused_cluster"
+
+
+def test_mid_grid_defaults_to_small_tiles():
+    # 1100 x 500 points: 315 tiles of 32 x 60 are less than a wave of
+    # resident CTAs, so each step is one launch of 16 x 28 tiles.
+    from psvwave_gb300 import workloads
+
+    m = psv.fdModel.from_parameters(workloads.c3_params(nt=10, n_shots=1))
+    assert m.kernel_variant == "fused_tma"
+    assert m.tile_shape == "16x28"
