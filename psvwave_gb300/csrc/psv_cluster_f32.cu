@@ -264,11 +264,13 @@ int plan(int nx, int nz, int np) {
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
           cudaSuccess)
     return 0;
+  // The shared-memory limit is an attribute of the kernel, shared by every
+  // model: set it to the device's maximum, not to this grid's need.
   for (int nc : {16, 8}) {
     if (nx < 2 * nc) continue;
     const size_t smem = smem_bytes(max_rows(nc, nx), stride(nz), np);
     if (smem > (size_t)optin) continue;
-    if (!configure<false>(smem, nc) || !configure<true>(smem, nc)) continue;
+    if (!configure<false>((size_t)optin, nc) || !configure<true>((size_t)optin, nc)) continue;
     if (placeable<false>(smem, nc) && placeable<true>(smem, nc)) return nc;
   }
   cudaGetLastError();  // a refused non-portable size is not an error here

@@ -135,3 +135,22 @@ def test_tiny_grid_fp32_schemes_within_tolerance(case, variant, shape):
             assert rel_l2(out[k], ref[k]) <= 1e-4, k
         else:
             assert not out[k].any(), k
+
+
+def test_cluster_models_of_different_sizes_coexist(golden):
+    """The cluster kernel's shared-memory limit is a property of the kernel,
+    shared by every model: a 250 x 150 model built first still runs after a
+    16 x 14 model (a few KB per CTA) is built, and agrees with its first
+    run bit for bit."""
+    from psvwave_gb300 import workloads
+
+    big = psv.fdModel.from_parameters(workloads.c0_params())
+    big.set_parameter_fields(*workloads.c0_media()[0])
+    assert big.kernel_variant == "fused_cluster"
+    big.forward_simulate(0, False)
+    first = big.get_synthetic_data()[0].copy()
+    small = psv.fdModel.from_parameters(CASES["16x14"])
+    assert small.kernel_variant == "fused_cluster"
+    small.forward_simulate(0, False)
+    big.forward_simulate(0, False)
+    assert np.array_equal(big.get_synthetic_data()[0], first)
