@@ -92,11 +92,158 @@ __device__ __forceinline__ bool interior_tile(const SimDesc &d, int X0, int Z0, 
          Z0 + S::TZ + 1 <= min(d.nz - 3, d.nz - d.np);
 }
 
+// A taper tile has every stress point of its box inside the updated region
+// but lies (partly) in the absorbing frame; no source or snapshot I/O. It
+// takes the interior path with the taper factor applied.
+template <class S>
+__device__ __forceinline__ bool taper_tile(const SimDesc &d, int X0, int Z0, bool snap_io) {
+  const InjPlan &p = d.plan;
+  const bool inj = p.n && X0 < p.x0 + p.w && p.x0 < X0 + S::TX && Z0 < p.z0 + p.h &&
+                   p.z0 < Z0 + S::TZ;
+  return !snap_io && !inj && X0 - 2 >= 2 && Z0 - 2 >= 2 && X0 + S::TX + 1 <= d.nx - 3 &&
+         Z0 + S::TZ + 1 <= d.nz - 3;
+}
+
+// Taper factor of grid point (gx, gz) from the column factor tzc: the table
+// at the point's frame count min(tz, tx) (1 from np frames on) is the
+// smaller of the table at tz and at tx, since the Cerjan taper grows with
+// the count.
+__device__ __forceinline__ float row_taper(const SimDesc &d, int gx) {
+  const int tx = min(gx + 1, d.nx - gx);
+  return tx < d.np ? __ldg(d.taper_tab + tx) : 1.0f;
+}
+__device__ __forceinline__ float col_taper(const SimDesc &d, int gz) {
+  const int tz = min(gz + 1, d.nz - gz);
+  return tz < d.np ? __ldg(d.taper_tab + tz) : 1.0f;
+}
+
+// Phases B and C of an interior tile (TAPER false: taper exactly 1) or a
+// taper tile (TAPER true). Phase B: each thread walks SR / G consecutive
+// rows of one column, keeping the x-direction stencil values of vx and vz in
+// registers (one new shared load each per row); phase C: KC consecutive
+// rows per thread with the x-direction windows of txx and txz.
+template <class S, bool ADJ, bool TAPER>
+__device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields &out, int X0,
+                                            int Z0, const float (*VX)[S::W],
+                                            const float (*VZ)[S::W], float (*sxx_)[S::W],
+                                            float (*szz_)[S::W], float (*sxz_)[S::W],
+                                            const float (*slm)[S::W], const float (*smu)[S::W],
+                                            const float *bb) {
+  constexpr int TX = S::TX, TZ = S::TZ, SR = S::SR, G = S::G;
+  constexpr int KC = TX / G;
+  const int ps = d.pitch;
+  const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
+  const float dtv = ADJ ? -d.dt : d.dt;
+  const float idx = d.idx, idz = d.idz;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = w % S::H, q = w / S::H;
+  const int lzc = h * 32 + lane;
+  const int gzc = Z0 + lzc;
+  {
+    constexpr int RB = SR / G;
+    const int c = 2 + h * 32 + lane;
+    const int gz = Z0 - 4 + c;
+    const bool z_own = c >= 4 && c < TZ + 4;
+    const int r0 = q * RB;
+    const float tzc = TAPER ? col_taper(d, gz) : 1.0f;
+    float xm1 = VX[r0 + 1][c], x0 = VX[r0 + 2][c], xp1 = VX[r0 + 3][c], xp2 = VX[r0 + 4][c];
+    float zm2 = VZ[r0][c], zm1 = VZ[r0 + 1][c], z0 = VZ[r0 + 2][c], zp1 = VZ[r0 + 3][c];
+    int gp = (X0 - 2 + r0) * ps + gz;
+#pragma unroll
+    for (int k = 0; k < RB; ++k) {
+      const int r = r0 + k, vr = r + 2;
+      const float lm = slm[r][c], mu = smu[r][c];
+      const float la = lm - 2.0f * mu;
+      const float dvx = c1 * (xp1 - x0) + c2 * (xm1 - xp2);
+      const float dvz = c1 * (z0 - VZ[vr][c - 1]) + c2 * (VZ[vr][c - 2] - VZ[vr][c + 1]);
+      const float gxz = (c1 * (VX[vr][c + 1] - x0) + c2 * (VX[vr][c - 1] - VX[vr][c + 2])) * idz +
+                        (c1 * (z0 - zm1) + c2 * (zm2 - zp1)) * idx;
+      const float ex = dvx * idx, ez = dvz * idz;
+      float sxx, szz, sxz;
+      if (TAPER) {
+        const float tp = fminf(tzc, row_taper(d, X0 - 2 + r));
+        sxx = tp * (sxx_[r][c] + dtv * (lm * ex + la * ez));
+        szz = tp * (szz_[r][c] + dtv * (la * ex + lm * ez));
+        sxz = tp * (sxz_[r][c] + dtv * mu * gxz);
+      } else {
+        sxx = sxx_[r][c] + dtv * (lm * ex + la * ez);
+        szz = szz_[r][c] + dtv * (la * ex + lm * ez);
+        sxz = sxz_[r][c] + dtv * mu * gxz;
+      }
+      sxx_[r][c] = sxx;
+      szz_[r][c] = szz;
+      sxz_[r][c] = sxz;
+      if (z_own && r >= 2 && r < TX + 2) {
+        out.txx[gp] = sxx;
+        out.tzz[gp] = szz;
+        out.txz[gp] = sxz;
+      }
+      gp += ps;
+      if (k + 1 < RB) {
+        xm1 = x0;
+        x0 = xp1;
+        xp1 = xp2;
+        xp2 = VX[vr + 3][c];
+        zm2 = zm1;
+        zm1 = z0;
+        z0 = zp1;
+        zp1 = VZ[vr + 2][c];
+      }
+    }
+  }
+  __syncthreads();
+  if (lzc < TZ) {
+    const float(*TXX)[S::W] = sxx_;
+    const float(*TZZ)[S::W] = szz_;
+    const float(*TXZ)[S::W] = sxz_;
+    const int cc = lzc + 4;
+    const int lx0 = q * KC;
+    const int s0 = lx0 + 2;  // stress box row of the first point
+    const float tzc = TAPER ? col_taper(d, gzc) : 1.0f;
+    float am2 = TXX[s0 - 2][cc], am1 = TXX[s0 - 1][cc], a0 = TXX[s0][cc], ap1 = TXX[s0 + 1][cc];
+    float bm1 = TXZ[s0 - 1][cc], b0 = TXZ[s0][cc], bp1 = TXZ[s0 + 1][cc], bp2 = TXZ[s0 + 2][cc];
+    int gq = (X0 + lx0) * ps + gzc;
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+      const int r = s0 + k, lx = lx0 + k;
+      const float ax = (c1 * (a0 - am1) + c2 * (am2 - ap1)) * idx +
+                       (c1 * (b0 - TXZ[r][cc - 1]) + c2 * (TXZ[r][cc - 2] - TXZ[r][cc + 1])) * idz;
+      const float az = (c1 * (bp1 - b0) + c2 * (bm1 - bp2)) * idx +
+                       (c1 * (TZZ[r][cc + 1] - TZZ[r][cc]) + c2 * (TZZ[r][cc - 1] - TZZ[r][cc + 2])) * idz;
+      const float bdt = bb[k] * dtv;
+      if (TAPER) {
+        const float tp = fminf(tzc, row_taper(d, X0 + lx));
+        out.vx[gq] = tp * (VX[lx + 4][cc] + bdt * ax);
+        out.vz[gq] = tp * (VZ[lx + 4][cc] + bdt * az);
+      } else {
+        out.vx[gq] = VX[lx + 4][cc] + bdt * ax;
+        out.vz[gq] = VZ[lx + 4][cc] + bdt * az;
+      }
+      gq += ps;
+      if (k + 1 < KC) {
+        am2 = am1;
+        am1 = a0;
+        a0 = ap1;
+        ap1 = TXX[r + 2][cc];
+        bm1 = b0;
+        b0 = bp1;
+        bp1 = bp2;
+        bp2 = TXZ[r + 3][cc];
+      }
+    }
+  }
+}
+
 // One tile's time step. `maps` are the tensor maps of this step's input set;
 // the kernels below pass them either as a kernel parameter (single model:
 // the copies can be issued without waiting for any load) or from the
 // descriptor table (batch).
-template <class S, int CFG, bool ADJ>
+// TAPERED: taper tiles take the interior path with the taper factor. On for
+// the 128-thread shapes (small and mid-size grids, where the absorbing frame
+// holds many tiles: +3.5 % on the batched and surrogate workloads); off for
+// 32 x 60, whose 2100 x 900 persistent step it slowed by 1.5 %. A shape
+// uses the same paths in every kernel, so per-step and persistent launches
+// give the same bits.
+template <class S, int CFG, bool ADJ, bool TAPERED = (S::NT == 128)>
 __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, int X0, int Z0,
                                           bool first, int tile, int it, int parity, int store,
                                           int *err, uint32_t phase, bool init_bar,
@@ -131,6 +278,7 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   const bool snap_io = (it % d.si) == 0 && d.accu[0] != nullptr && (ADJ || store);
   const size_t soff = (size_t)(it / d.si) * nx * nz;
   const bool inner = interior_tile<S>(d, X0, Z0, snap_io);
+  const bool tapered = TAPERED && !inner && taper_tile<S>(d, X0, Z0, snap_io);
 
   // This thread's buoyancy values for phase C (the medium does not change
   // between steps, so they load before the previous step has finished).
@@ -144,7 +292,7 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   float bb[KC];
 #pragma unroll
   for (int k = 0; k < KC; ++k) {
-    const int gx = inner ? X0 + q * KC + k : X0 + q + G * k;
+    const int gx = (inner || tapered) ? X0 + q * KC + k : X0 + q + G * k;
     bb[k] = (col_ok && gx < nx) ? __ldg(d.b + gx * ps + gzc) : 0.f;
   }
   griddep_wait();
@@ -209,86 +357,11 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   const float(*VZ)[W] = sv1;
 
   if (inner) {
-    // Phase B, interior: each thread walks SR / G consecutive rows of one
-    // column, keeping the x-direction stencil values of vx and vz in
-    // registers (one new shared load each per row).
-    constexpr int RB = SR / G;
-    const int c = 2 + h * 32 + lane;
-    const int gz = Z0 - 4 + c;
-    const bool z_own = c >= 4 && c < TZ + 4;
-    const int r0 = q * RB;
-    float xm1 = VX[r0 + 1][c], x0 = VX[r0 + 2][c], xp1 = VX[r0 + 3][c], xp2 = VX[r0 + 4][c];
-    float zm2 = VZ[r0][c], zm1 = VZ[r0 + 1][c], z0 = VZ[r0 + 2][c], zp1 = VZ[r0 + 3][c];
-    int gp = (X0 - 2 + r0) * ps + gz;
-#pragma unroll
-    for (int k = 0; k < RB; ++k) {
-      const int r = r0 + k, vr = r + 2;
-      const float lm = slm[r][c], mu = smu[r][c];
-      const float la = lm - 2.0f * mu;
-      const float dvx = c1 * (xp1 - x0) + c2 * (xm1 - xp2);
-      const float dvz = c1 * (z0 - VZ[vr][c - 1]) + c2 * (VZ[vr][c - 2] - VZ[vr][c + 1]);
-      const float gxz = (c1 * (VX[vr][c + 1] - x0) + c2 * (VX[vr][c - 1] - VX[vr][c + 2])) * idz +
-                        (c1 * (z0 - zm1) + c2 * (zm2 - zp1)) * idx;
-      const float ex = dvx * idx, ez = dvz * idz;
-      const float sxx = sxx_[r][c] + dtv * (lm * ex + la * ez);
-      const float szz = szz_[r][c] + dtv * (la * ex + lm * ez);
-      const float sxz = sxz_[r][c] + dtv * mu * gxz;
-      sxx_[r][c] = sxx;
-      szz_[r][c] = szz;
-      sxz_[r][c] = sxz;
-      if (z_own && r >= 2 && r < TX + 2) {
-        out.txx[gp] = sxx;
-        out.tzz[gp] = szz;
-        out.txz[gp] = sxz;
-      }
-      gp += ps;
-      if (k + 1 < RB) {
-        xm1 = x0;
-        x0 = xp1;
-        xp1 = xp2;
-        xp2 = VX[vr + 3][c];
-        zm2 = zm1;
-        zm1 = z0;
-        z0 = zp1;
-        zp1 = VZ[vr + 2][c];
-      }
-    }
-    __syncthreads();
-    // Phase C, interior: KC consecutive rows per thread with the x-direction
-    // windows of txx and txz in registers.
-    if (lzc < TZ) {
-      const float(*TXX)[W] = sxx_;
-      const float(*TZZ)[W] = szz_;
-      const float(*TXZ)[W] = sxz_;
-      const int cc = lzc + 4;
-      const int lx0 = q * KC;
-      const int s0 = lx0 + 2;  // stress box row of the first point
-      float am2 = TXX[s0 - 2][cc], am1 = TXX[s0 - 1][cc], a0 = TXX[s0][cc], ap1 = TXX[s0 + 1][cc];
-      float bm1 = TXZ[s0 - 1][cc], b0 = TXZ[s0][cc], bp1 = TXZ[s0 + 1][cc], bp2 = TXZ[s0 + 2][cc];
-      int gq = (X0 + lx0) * ps + gzc;
-#pragma unroll
-      for (int k = 0; k < KC; ++k) {
-        const int r = s0 + k, lx = lx0 + k;
-        const float ax = (c1 * (a0 - am1) + c2 * (am2 - ap1)) * idx +
-                         (c1 * (b0 - TXZ[r][cc - 1]) + c2 * (TXZ[r][cc - 2] - TXZ[r][cc + 1])) * idz;
-        const float az = (c1 * (bp1 - b0) + c2 * (bm1 - bp2)) * idx +
-                         (c1 * (TZZ[r][cc + 1] - TZZ[r][cc]) + c2 * (TZZ[r][cc - 1] - TZZ[r][cc + 2])) * idz;
-        const float bdt = bb[k] * dtv;
-        out.vx[gq] = VX[lx + 4][cc] + bdt * ax;
-        out.vz[gq] = VZ[lx + 4][cc] + bdt * az;
-        gq += ps;
-        if (k + 1 < KC) {
-          am2 = am1;
-          am1 = a0;
-          a0 = ap1;
-          ap1 = TXX[r + 2][cc];
-          bm1 = b0;
-          b0 = bp1;
-          bp1 = bp2;
-          bp2 = TXZ[r + 3][cc];
-        }
-      }
-    }
+    tile_phases<S, ADJ, false>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
+    return true;
+  }
+  if (TAPERED && tapered) {
+    tile_phases<S, ADJ, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
     return true;
   }
 
@@ -502,8 +575,8 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
     if (j > 0 && threadIdx.x == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
     const int it = ADJ ? it0 - j : it0 + j;
     const int parity = parity0 ^ (j & 1);
-    if (!step_body<S, CFG, ADJ>(d, d.maps[parity], tx * S::TX, tz * S::TZ, false, tile, it, parity,
-                                store, err, phase, init, init))
+    if (!step_body<S, CFG, ADJ>(d, d.maps[parity], tx * S::TX, tz * S::TZ, false, tile, it,
+                                parity, store, err, phase, init, init))
       return;
     phase ^= 1u;
     init = false;
