@@ -296,12 +296,13 @@ __global__ void narrow_kernel(size_t n, const double *src, T *dst) {
 
 namespace kern {
 // Rows of the two-kernel step's 32-column CTAs. FP64 keeps the FP64 pipe
-// busy on every SM it has work on, so small CTAs (2 rows) spread the grid
-// evenly over the SMs: at 250 x 150, 32 x 8 CTAs made 160 CTAs for 152 SMs
-// and eight SMs ran two, doubling the step; 32 x 2 CTAs make 625.
+// busy on every SM it has work on, so small CTAs spread the grid evenly over
+// the SMs: at 250 x 150, 32 x 8 CTAs made 160 CTAs for 152 SMs and eight
+// SMs ran two, doubling the step; one-row CTAs make 1250 (c0 FP64 gradient
+// 174 ms with 32 x 8, 144 ms with 32 x 2, 141 ms with 32 x 1).
 template <typename T>
 struct BlockRows {
-  static constexpr int value = sizeof(T) == 8 ? 2 : 8;
+  static constexpr int value = sizeof(T) == 8 ? 1 : 8;
 };
 }  // namespace kern
 
