@@ -19,11 +19,23 @@
 // A TMA copy must start on a 16-byte boundary of the innermost (z) axis:
 // every box starts at z = Z0 - 4 with Z0 a multiple of TZ (TZ a multiple of
 // 4) and is TZ + 8 points wide; rows are padded to a multiple of 4 points.
-// Warps of the compute phases own 32 consecutive z columns and walk every
-// G-th row, so column arithmetic happens once per thread.
+// Warps of the compute phases own 32 consecutive z columns. Three kinds of
+// tile take three paths: interior tiles (taper exactly 1, no per-point
+// tests) and, on the 128-thread shapes, taper tiles (inside the updated
+// region, in the absorbing frame) walk consecutive rows with the x-direction
+// stencil values in registers; the others walk every G-th row with
+// per-point bounds and taper tests. Tile shapes: 32 x 60 (256 threads),
+// 16 x 28 and 20 x 28 (128 threads).
 //
-// The mbarrier wait is bounded: on time-out the CTA raises the error flag,
-// waits (bounded again) for its copies to land, and returns.
+// Launch schemes: one launch per time step (fused_step_tma, and
+// fused_step_tma_batch over a tile table), or every step in one persistent
+// cooperative launch (fused_steps_tma, fused_steps_tma_batch) whose CTAs
+// take (step, tile) items in step order, start an item once the tile and
+// its neighbours have published the previous step, and publish with a
+// barrier plus one release store.
+//
+// Every wait is bounded: on time-out the CTA raises the error flag, waits
+// (bounded again) for its copies to land, and returns.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
