@@ -313,6 +313,10 @@ int psv_batch_add(psv_batch *b, psv_model *m, int i_shot);
  * n_steps <= 0). */
 int psv_batch_forward(psv_batch *b, int store_fields, int n_steps);
 int psv_batch_set_tile_shape(psv_batch *b, int shape);
+/* psv_batch_autotune times every tile shape with both launch schemes (one
+ * launch per step, persistent) on n_steps steps of the active members, keeps
+ * the fastest pair and returns its shape in *chosen (the scheme is read
+ * with psv_batch_get_persistent). */
 int psv_batch_autotune(psv_batch *b, int n_steps, int *chosen);
 int psv_batch_info(const psv_batch *b, int *members, int *tiles, double *cells);
 /* Which members (in the order added) the next psv_batch_forward advances:
@@ -325,6 +329,7 @@ int psv_batch_set_active(psv_batch *b, const int *flags, int n);
  * table, tiles starting a step as soon as their neighbours have finished the
  * previous one. Results are identical. */
 int psv_batch_set_persistent(psv_batch *b, int persistent);
+int psv_batch_get_persistent(const psv_batch *b, int *persistent);
 
 /* ---- no-allocation entry point ------------------------------------------ */
 /* L2 misfit 0.5 dt sum((obs - syn)^2) over both components, written to the

@@ -40,7 +40,9 @@ class Batch:
 
     @property
     def persistent(self):
-        return getattr(self, "_persistent", False)
+        v = ctypes.c_int()
+        _capi.check(self._lib.psv_batch_get_persistent(self._h, ctypes.byref(v)))
+        return bool(v.value)
 
     @persistent.setter
     def persistent(self, on):
@@ -48,7 +50,6 @@ class Batch:
         (False, the default), or every step in one persistent launch (True).
         Results are identical."""
         _capi.check(self._lib.psv_batch_set_persistent(self._h, int(bool(on))))
-        self._persistent = bool(on)
 
     def set_active(self, mask=None):
         """Members the next forward() advances (a boolean per member, in the
@@ -74,6 +75,9 @@ class Batch:
         self._tile_shape = name
 
     def autotune(self, n_steps=50):
+        """Times every tile shape with both launch schemes on n_steps steps
+        of the active members and keeps the fastest pair; returns the shape
+        (the scheme is `persistent`)."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_batch_autotune(self._h, int(n_steps), ctypes.byref(v)))
         self._tile_shape = {0: "32x60", 1: "16x28", 2: "20x28"}[v.value]

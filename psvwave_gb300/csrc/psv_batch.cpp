@@ -287,28 +287,38 @@ void Batch::forward(bool store, int n_steps) {
 
 int Batch::autotune(int n_steps) {
   if (members_.empty()) return tile_cfg_;
+  // Every (launch scheme, tile shape) pair on n_steps steps of the members
+  // currently active, each timed on its third run (after the build and the
+  // graph capture); the fastest pair is kept.
   float best = 0;
   int best_cfg = tile_cfg_;
+  bool best_persistent = persistent_, first = true;
   cudaEvent_t a, b;
   cuda_check(cudaEventCreate(&a), "cudaEventCreate");
   cuda_check(cudaEventCreate(&b), "cudaEventCreate");
-  for (int cfg = 0; cfg < tma::kNumTileCfgs; ++cfg) {
-    set_tile_cfg(cfg);
-    forward(false, n_steps);  // eager run (also builds)
-    forward(false, n_steps);  // graph capture
-    cudaEventRecord(a, stream_);
-    forward(false, n_steps);
-    cudaEventRecord(b, stream_);
-    cudaEventSynchronize(b);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, a, b);
-    if (cfg == 0 || ms < best) {
-      best = ms;
-      best_cfg = cfg;
+  for (bool p : {false, true}) {
+    for (int cfg = 0; cfg < tma::kNumTileCfgs; ++cfg) {
+      set_persistent(p);
+      set_tile_cfg(cfg);
+      forward(false, n_steps);  // eager run (also builds)
+      forward(false, n_steps);  // graph capture
+      cudaEventRecord(a, stream_);
+      forward(false, n_steps);
+      cudaEventRecord(b, stream_);
+      cudaEventSynchronize(b);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      if (first || ms < best) {
+        best = ms;
+        best_cfg = cfg;
+        best_persistent = p;
+        first = false;
+      }
     }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  set_persistent(best_persistent);
   set_tile_cfg(best_cfg);
   return best_cfg;
 }

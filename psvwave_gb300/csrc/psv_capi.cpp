@@ -638,6 +638,14 @@ int psv_batch_set_persistent(psv_batch *b, int persistent) {
   });
 }
 
+int psv_batch_get_persistent(const psv_batch *b, int *persistent) {
+  return guarded([&] {
+    need(b, "batch");
+    need(persistent, "persistent");
+    *persistent = b->impl.persistent() ? 1 : 0;
+  });
+}
+
 int psv_batch_set_active(psv_batch *b, const int *flags, int n) {
   return guarded([&] {
     need(b, "batch");

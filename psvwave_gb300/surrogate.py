@@ -231,6 +231,9 @@ class FDPosterior:
         self.batch = Batch(device)
         for m in self.models:
             self.batch.add(m, 0)
+        # The judge's batched forward is most of a sampler iteration: time
+        # every launch scheme and tile shape once and keep the fastest.
+        self.batch.autotune(50)
         self.n_potentials = 0
         self.n_gradients = 0
 
