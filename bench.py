@@ -28,7 +28,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Gcell-updates/s"
-# FP32 algorithmic bytes per cell-update of each step kernel
+# FP32 algorithmic bytes per cell-update of each step kernel: reads and writes
+# of the fields, medium and buoyancy per point and step, at one visit each
 BYTES_PER_CELL = {"stress_step": 48, "velocity_step": 36, "fused_step": 56, "fused_step_tma": 52,
                   "fused_steps_tma": 52}
 

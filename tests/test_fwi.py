@@ -26,7 +26,7 @@ def test_gradient_vector_matches_the_model_vector_basis(golden):
 
 
 class _Quadratic:
-    """f(m) = 0.5 |m - m*|^2 with the fdModel calls the driver makes."""
+    """f(m) = 0.5 |m - m*|^2 with the fdModel calls the L-BFGS-B loop makes."""
 
     def __init__(self, n, seed=0):
         rng = np.random.default_rng(seed)
