@@ -46,6 +46,9 @@ def parse():
                    help="skip the FWI-gradient and batching measurements")
     p.add_argument("--ncu-case", type=int, default=0, metavar="NT",
                    help="run one NT-step forward of the c1 workload and exit (for ncu captures)")
+    p.add_argument("--ncu-case-small", type=int, default=0, metavar="NT",
+                   help="run one NT-step forward of the c0 workload (the default scheme there: "
+                        "cluster-resident), launch by launch, and exit (for ncu captures)")
     p.add_argument("--ncu-case-exact", type=int, default=0, metavar="NT",
                    help="run one exact gradient of one NT-step shot of the c3 workload, launch by "
                         "launch, and exit (for ncu captures)")
@@ -360,6 +363,22 @@ def ncu_case(nt):
         m.kernel_variant, m.tile_shape, m.get_synthetic_data()[0].sum()))
 
 
+def ncu_case_small(nt):
+    """A short forward of the c0 workload with its default scheme, kernels
+    launched one by one (no graph), for ncu captures."""
+    import psvwave_gb300 as psv
+    from psvwave_gb300 import workloads
+
+    p = workloads.c0_params()
+    p["nt"] = nt
+    m = psv.fdModel.from_parameters(p)
+    m.set_graph_capture(False)
+    m.set_parameter_fields(*workloads.c0_media()[0])
+    m.forward_simulate(0, False)
+    print("ncu small case: %s, seismogram sum %.6e" % (m.kernel_variant,
+                                                      m.get_synthetic_data()[0].sum()))
+
+
 def ncu_case_exact(nt):
     """One exact gradient (checkpoints every 100 steps) of a one-shot, NT-step
     version of the c3 workload, kernels launched one by one (no graph), for
@@ -385,6 +404,9 @@ def main():
         return
     if args.ncu_case_exact:
         ncu_case_exact(args.ncu_case_exact)
+        return
+    if args.ncu_case_small:
+        ncu_case_small(args.ncu_case_small)
         return
     if args.impl == "reference":
         run_reference(args)
