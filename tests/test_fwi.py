@@ -57,3 +57,34 @@ def test_lbfgs_driver_converges_and_computes_each_vector_once():
     # misfit and grad at the same vector share one computation.
     assert problem.evaluations == q.runs == res.nfev
     assert [h[0] for h in problem.history][0] == 0.5 * float(np.sum(q.target ** 2))
+
+
+class _Blocks(_Quadratic):
+    """The quadratic stand-in with the model-vector geometry attributes:
+    12 x 8 free cells, one point per block, vector [vp | vs | rho]."""
+
+    nx_free_parameters, nz_free_parameters, npx, npz = 12, 8, 1, 1
+
+    def __init__(self):
+        super().__init__(3 * 12 * 8)
+
+
+def test_gradient_smoothing_follows_the_model_vector_layout():
+    """With smoothing, each parameter's block of the gradient is filtered as
+    an image of nz_free x nx_free (index bx + bz * nx_free, the reference
+    workflow's reshape): a gradient concentrated at one block spreads
+    symmetrically in x and z around it, and stays within its parameter."""
+    q = _Blocks()
+    bx, bz, nxb = 5, 3, 12
+    q.target[:] = 0.0
+    q.m = np.zeros_like(q.target)
+    q.m[96 + bx + bz * nxb] = 1.0  # vs block, one cell
+    g = fwi.FWI(q, smoothing=1.0).grad(q.m)
+    vp, vs, rho = np.split(g, 3)
+    assert not vp.any() and not rho.any()
+    img = vs.reshape(8, 12)
+    assert np.unravel_index(np.argmax(img), img.shape) == (bz, bx)
+    assert np.isclose(img[bz, bx - 1], img[bz, bx + 1])
+    assert np.isclose(img[bz - 1, bx], img[bz + 1, bx])
+    assert np.isclose(img[bz, bx + 1], img[bz + 1, bx])  # isotropic filter
+    assert np.isclose(img.sum(), 1.0)
