@@ -17,9 +17,12 @@
 //   phase 3: per own point, tau-bar = T lt~, v-bar = T lv + E^T p plus the
 //            receiver terms of the point (in increasing receiver index), and
 //            the gradient terms, added to sums loaded right after the wait.
-// The adjoint state is computed with exactly the expressions of
-// exact::exact_step_tile<float> and exact::add_receiver_terms (the same
-// bits). The gradient terms are formed in FP32 and summed in float-float
+// The adjoint state is computed with the expressions of
+// exact::exact_step_tile<float> and exact::add_receiver_terms: the general
+// path gives the same bits; the interior path below drops the taper factor
+// (exactly 1), so the compiler fuses a few products differently there
+// (about 4e-7 relative on a gradient). The gradient terms are formed in
+// FP32 and summed in float-float
 // pairs (hi, lo) with Knuth's TwoSum (The Art of Computer Programming,
 // vol. 2, 4.2.2), which carries each addition's rounding error exactly into
 // lo: about 48 significant bits, like the FP64 sums of exact_step_tile, but
