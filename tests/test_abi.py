@@ -129,3 +129,20 @@ def test_fdmodel_without_gpu_fails_loudly():
         pytest.skip("a GPU is present")
     with pytest.raises(_capi.PsvError, match="CUDA"):
         psvwave_gb300.fdModel(SMALL_INI)
+
+
+def test_empty_receiver_list_rejected_like_the_reference(tmp_path):
+    """An INI with nr = 0 and empty receiver lists is refused, with the
+    reference's message (its parser does the same)."""
+    from oracle import refbind
+    from tests.test_oracle import _tiny_ini
+
+    p = tmp_path / "no_receivers.ini"
+    p.write_text(_tiny_ini(12, 8, 3, [(5, 4, 60.0)], [], [[0]]))
+    info = _capi.PsvInfo()
+    assert _capi.load().psv_config_info(str(p).encode(), ctypes.byref(info)) == 1
+    msg = _capi.load().psv_last_error().decode()
+    assert "Mismatch between nr and receivers" in msg
+    if refbind.available():
+        with pytest.raises(Exception, match="Mismatch between nr and receivers"):
+            refbind.RefModel(str(p))
