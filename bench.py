@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark of the P-SV forward solver: Gcell-updates/s on the 2100 x 900
 grid (2000 x 800 inner cells + 50-cell Cerjan boundary), 5000 time steps,
-400 receivers, one dipping source, FP32 wave fields, seeded layered
+400 receivers, one explosive + dip source, FP32 wave fields, seeded layered
 Gaussian-random medium (psvwave_gb300/workloads.py, c1).
 
 A step is one complete forward simulation (forward_simulate of shot 0, no
@@ -131,15 +131,18 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def cpu_baseline(params_fn, media, seconds=12.0):
+def cpu_baseline(params_fn, media, seconds=12.0, moment=None):
     """The oracle port (the reference's algorithm in C/OpenMP) on a bounded
-    sample of the workload: the same grid and medium, fewer time steps."""
+    sample of the workload: the same grid, source and medium, fewer time
+    steps."""
     from oracle import portbind
 
     def run(n):
         p = params_fn(nt=n)
         p["snapshot_interval"] = n
         o = portbind.OracleModel(params=p)
+        if moment is not None:
+            o.view("moment")[...] = moment
         o.set_parameter_fields(*media)
         t = time.perf_counter()
         o.forward_simulate(0, False)
@@ -333,7 +336,7 @@ def run_reference(args):
     samples = []
     base = None
     for i in range(args.warmup + args.steps):
-        b = cpu_baseline(workloads.c1_params, media, seconds=5.0)
+        b = cpu_baseline(workloads.c1_params, media, seconds=5.0, moment=workloads.c1_moment())
         if i >= args.warmup:
             samples.append(b["value"])
             base = b
@@ -356,8 +359,7 @@ def ncu_case(nt):
     import psvwave_gb300 as psv
     from psvwave_gb300 import workloads
 
-    m = psv.fdModel.from_parameters(workloads.c1_params(nt=nt))
-    m.set_parameter_fields(*workloads.c1_media())
+    m = workloads.c1_model(nt=nt)
     m.forward_simulate(0, False)
     print("ncu case: %s, %s tiles, seismogram sum %.6e" % (
         m.kernel_variant, m.tile_shape, m.get_synthetic_data()[0].sum()))
@@ -425,12 +427,10 @@ def main():
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
 
-    params = workloads.c1_params()
     media = workloads.c1_media(seed=1 + rank)
-    model = psv.fdModel.from_parameters(params, precision=args.precision, device=local_rank)
+    model = workloads.c1_model(precision=args.precision, device=local_rank, seed=1 + rank)
     stream = torch.cuda.Stream(device=dev)
     model.set_stream(stream.cuda_stream)
-    model.set_parameter_fields(*media)
     cells = model.nx * model.nz
     nt = model.nt
     work = cells * nt
@@ -495,6 +495,18 @@ def main():
     h2d = 3 * cells * 8
     d2h = 2 * model.n_shots * model.nr * model.nt * 8
 
+    # The FP32 answer against the FP64 solve of the same run (outside every
+    # timed region): relative L2 error of both seismogram components.
+    parity = None
+    if rank == 0 and args.precision == "fp32":
+        m64 = workloads.c1_model(precision="fp64", device=local_rank, seed=1 + rank)
+        m64.forward_simulate(0, False)
+        errs = [float(np.linalg.norm(a - b) / np.linalg.norm(b))
+                for a, b in zip((ux, uz), m64.get_synthetic_data())]
+        parity = {"against": "FP64 GPU solve of the same 5000-step run",
+                  "seismogram_rel_l2": {"ux": errs[0], "uz": errs[1]}, "tolerance": 1e-4}
+        del m64
+
     # Roofline of the dominant kernel, per time step: the timed region's
     # device time divided by its time steps (each timed forward also holds
     # one field memset and the receiver prefix sum, so the figure is
@@ -530,7 +542,7 @@ def main():
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        base = cpu_baseline(workloads.c1_params, media)
+        base = cpu_baseline(workloads.c1_params, media, moment=workloads.c1_moment())
     secondary = None
     if rank == 0 and not args.no_secondary:
         secondary = {"fwi_gradients": fwi_gradients(args.steps, args.warmup,
@@ -556,6 +568,7 @@ def main():
             "roofline": roofline,
             "cpu_baseline": base,
             "clocks": clocks,
+            "parity": parity,
             "secondary": secondary,
         }
         print(json.dumps(line), flush=True)

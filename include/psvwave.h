@@ -343,7 +343,11 @@ int psv_batch_get_persistent(const psv_batch *b, int *persistent);
  * array that every GPU loading this library holds until exit, so n is
  * limited to 16,777,216 samples; larger n returns PSV_ERR_INVALID_ARGUMENT.
  * The first call on a device (made current by the caller) looks up that
- * array's address; make that first call before any stream capture. All calls
+ * array's address; make that first call before any stream capture. The
+ * address is kept per device ordinal for the life of the process: it
+ * belongs to the device's primary context (the one the CUDA runtime uses),
+ * so call this under that context, and not after cudaDeviceReset on the
+ * device, which unloads the array and leaves the kept address stale. All calls
  * share the array: calls that overlap on the GPU race and must be ordered
  * (one stream, or events) by the caller. Asynchronous: the result is ready
  * when `stream` reaches it. */

@@ -30,13 +30,24 @@ def build_port(force=False):
     return PORT_LIB
 
 
+# Where the reference checkout's sources lie on the machine that made the
+# fixtures (read-only there); REF_SRC overrides it. Machines without the
+# checkout (the GPU hosts) skip the reference build.
+REF_CHECKOUT_SRC = "/root/reference/src"
+
+
+def ref_src():
+    return os.environ.get("REF_SRC", REF_CHECKOUT_SRC)
+
+
 def build_ref():
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
+    env = dict(os.environ, REF_SRC=ref_src())
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")], env=env)
 
 
 def build_all():
     build_port()
-    if os.path.isdir(os.environ.get("REF_SRC", "/root/reference/src")):
+    if os.path.isfile(os.path.join(ref_src(), "fdModel.cpp")):
         build_ref()
 
 

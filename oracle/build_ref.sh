@@ -4,14 +4,18 @@
 # as the maker of golden fixtures. Test infrastructure only.
 #
 # Inputs: the reference sources src/fdModel.cpp and src/contiguous_arrays.cpp
-# where they lie (REF_SRC, default /root/reference/src), plus the stand-in
+# where they lie (REF_SRC, required: the reference checkout's src/ folder;
+# oracle/build.py passes it), plus the stand-in
 # headers for the reference's absent Eigen and inih submodules in
 # oracle/ref_shim. Flags follow the reference's release build
 # (CMakeLists.txt: -O3, OpenMP, C++11-compatible code).
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF_SRC=${REF_SRC:-/root/reference/src}
 OUT="$HERE/_ref"
+if [ -z "$REF_SRC" ]; then
+  echo "build_ref.sh: set REF_SRC to the reference checkout's src/ folder" >&2
+  exit 2
+fi
 if [ ! -f "$REF_SRC/fdModel.cpp" ]; then
   echo "build_ref.sh: reference sources not found at $REF_SRC; skipping" >&2
   exit 0

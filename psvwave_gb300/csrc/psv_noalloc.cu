@@ -40,7 +40,9 @@ static __device__ __align__(256) double g_partials[kMaxPartials];
 
 namespace {
 
-// Device address of g_partials, looked up once per device.
+// Device address of g_partials, looked up once per device ordinal and kept
+// for the life of the process. It is the address in the device's primary
+// context; cudaDeviceReset unloads the module and makes it stale.
 double *g_partials_addr[kMaxDevices] = {};
 std::mutex g_setup_mutex;
 

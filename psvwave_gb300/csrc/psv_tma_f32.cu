@@ -725,7 +725,9 @@ cudaError_t launch_persistent(const SimDesc &d, int it0, int n_steps, int parity
   // CTAs would only hold items further ahead and poll for them.
   const long long slots = (long long)std::max(per_sm, 1) * sms;
   const int grid = (int)std::min(std::min<long long>(items, slots), 2LL * tiles_x * tiles_z);
-  if (items + grid >= 0x7fffffffLL) return cudaErrorInvalidValue;  // item numbers are 31-bit
+  // Item numbers are 31-bit: a CTA draws two numbers up front and one per
+  // item, so the counter reaches at most items + 2 * grid - 1.
+  if (items + 2LL * grid >= 0x7fffffffLL) return cudaErrorInvalidValue;
   // Cooperative launch: every CTA is resident at once, as CTAs that wait on
   // one another require.
   cudaLaunchAttribute attr[1];
@@ -929,7 +931,7 @@ cudaError_t launch_persistent_batch(const SimDesc *sims, const int4 *tiles, int 
   const long long items = (long long)n_steps * n_tiles;
   const long long slots = (long long)std::max(per_sm, 1) * sms;
   const int grid = (int)std::min(std::min<long long>(items, slots), 2LL * n_tiles);
-  if (items + grid >= 0x7fffffffLL) return cudaErrorInvalidValue;
+  if (items + 2LL * grid >= 0x7fffffffLL) return cudaErrorInvalidValue;  // 31-bit items
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;

@@ -11,8 +11,9 @@ media (vp, vs, rho on the padded [nx][nz] grid).
   nt = 5000; 30 horizontal layers with vp drawn uniformly in [1500, 4500]
   and sorted to increase with depth, vs = vp / 1.73, rho = 310 vp^0.25
   (Gardner), times a smooth Gaussian random field (sigma 5 %, correlation
-  length 40 cells); one dipping source (45 degrees), Ricker 15 Hz; 400
-  receivers along z = 5.
+  length 40 cells); one explosive + dip source (an isotropic tensor plus
+  the 45-degree dip tensor, c1_moment), Ricker 15 Hz; 400 receivers along
+  z = 5.
 * c2 -- many models of uneven sizes (c2_models).
 * c3 -- 1000 x 400 inner cells, 50-cell boundary, dx = dz = 5, dt = 4e-4
   (CFL number 0.59 at vp 4500), nt = 6000; 8 shots of one 45-degree source
@@ -59,6 +60,29 @@ def c1_params(nt=5000):
                 which_source_to_fire_in_which_shot=[[0]], nr=n_rec,
                 ix_receivers=[2 + 5 * k for k in range(n_rec)], iz_receivers=[5] * n_rec,
                 snapshot_interval=10)
+
+
+def c1_moment(dip_degrees=45.0):
+    """The explosive + dip source of c1 as one full moment tensor [1][2][2]:
+    an isotropic part diag(1, 1) plus the reference's dip-angle tensor
+    [[cos t, -sin t], [-sin t, -cos t]] (src/fdModel.cpp:233-246, with its
+    PI = 3.14159265), both scaled by 1e15 as the reference scales its
+    tensors. Set it with fdModel.set_moment after construction; the
+    reference's dip-angle parameterisation alone has no isotropic part."""
+    t = dip_degrees * 3.14159265 / 180.0
+    dip = np.array([[np.cos(t), -np.sin(t)], [-np.sin(t), -np.cos(t)]])
+    return ((np.eye(2) + dip) * 1e15)[None]
+
+
+def c1_model(nt=5000, precision="fp32", device=0, seed=1):
+    """An fdModel of the c1 workload: c1_params(nt), the explosive + dip
+    tensor of c1_moment, and the c1_media(seed) medium."""
+    from .model import fdModel
+
+    m = fdModel.from_parameters(c1_params(nt=nt), precision=precision, device=device)
+    m.set_moment(c1_moment())
+    m.set_parameter_fields(*c1_media(seed))
+    return m
 
 
 def gaussian_random_field(shape, corr_len, sigma, rng):

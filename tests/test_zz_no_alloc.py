@@ -62,3 +62,26 @@ def test_noalloc_misfit_rejects_oversize_input():
                                    ctypes.c_void_p(out.data_ptr()), None)
     assert rc == _capi.PSV_ERR_INVALID_ARGUMENT
     assert b"maximum of 16777216" in lib.psv_last_error()
+
+
+def test_noalloc_misfit_accepts_the_maximum_size():
+    """n at the stated maximum (every one of the 8192 partial sums in use)
+    is accepted and sums like a plain FP64 reduction of the same samples."""
+    torch = pytest.importorskip("torch")
+    lib = _capi.load()
+    g = torch.Generator(device="cuda:0")
+    g.manual_seed(7)
+    obs_ux, syn_ux, obs_uz, syn_uz = (
+        torch.randn(MAX_SAMPLES, dtype=torch.float64, device="cuda:0", generator=g)
+        for _ in range(4))
+    dt = 2.5e-4
+    expected = float(0.5 * dt * (((obs_ux - syn_ux) ** 2).sum() + ((obs_uz - syn_uz) ** 2).sum()))
+    out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda:0")
+    torch.cuda.synchronize()
+    rc = lib.psv_l2_misfit_noalloc(*[ctypes.c_void_p(t.data_ptr())
+                                     for t in (obs_ux, syn_ux, obs_uz, syn_uz)],
+                                   MAX_SAMPLES, dt, ctypes.c_void_p(out.data_ptr()), None)
+    assert rc == _capi.PSV_OK, lib.psv_last_error()
+    torch.cuda.synchronize()
+    got = float(out.item())
+    assert abs(got - expected) <= MISFIT_TOL * abs(expected), (got, expected)
