@@ -71,7 +71,7 @@ class Batch:
 
     @tile_shape.setter
     def tile_shape(self, name):
-        _capi.check(self._lib.psv_batch_set_tile_shape(self._h, {"32x60": 0, "16x28": 1, "20x28": 2}[name]))
+        _capi.check(self._lib.psv_batch_set_tile_shape(self._h, {"32x60": 0, "16x28": 1, "20x28": 2, "16x60": 3}[name]))
         self._tile_shape = name
 
     def autotune(self, n_steps=50):
@@ -80,7 +80,7 @@ class Batch:
         (the scheme is `persistent`)."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_batch_autotune(self._h, int(n_steps), ctypes.byref(v)))
-        self._tile_shape = {0: "32x60", 1: "16x28", 2: "20x28"}[v.value]
+        self._tile_shape = {0: "32x60", 1: "16x28", 2: "20x28", 3: "16x60"}[v.value]
         return self._tile_shape
 
     def info(self):

@@ -25,7 +25,7 @@ struct Maps {
 };
 
 // Tile shapes (x rows by z columns, threads per CTA).
-enum TileCfg { kTile32x60 = 0, kTile16x28 = 1, kTile20x28 = 2, kNumTileCfgs = 3 };
+enum TileCfg { kTile32x60 = 0, kTile16x28 = 1, kTile20x28 = 2, kTile16x60 = 3, kNumTileCfgs = 4 };
 void tile_dims(int cfg, int *tx, int *tz);
 
 // Everything a CTA needs about its simulation; lives in device memory.

@@ -50,9 +50,10 @@ namespace psv {
 namespace tma {
 namespace {
 
-template <int TX_, int TZ_, int NT_>
+template <int TX_, int TZ_, int NT_, int MINB_>
 struct Shape {
   static constexpr int TX = TX_, TZ = TZ_, NT = NT_;
+  static constexpr int MINB = MINB_;  // resident CTAs per SM the registers must allow
   static constexpr int W = TZ + 8;    // box width (z): Z0-4 .. Z0+TZ+4
   static constexpr int VR = TX + 8;   // velocity box rows: X0-4 .. X0+TX+4
   static constexpr int SR = TX + 4;   // stress / medium box rows: X0-2 .. X0+TX+2
@@ -71,9 +72,10 @@ struct Shape {
   static_assert(WARPS % H == 0 && SR % G == 0 && TX % G == 0, "row groups must tile the rows");
   static_assert(TZ % 4 == 0, "tile columns must keep TMA boxes 16-byte aligned");
 };
-using Big = Shape<32, 60, 256>;
-using Small = Shape<16, 28, 128>;
-using Mid = Shape<20, 28, 128>;
+using Big = Shape<32, 60, 256, 3>;
+using Small = Shape<16, 28, 128, 8>;
+using Mid = Shape<20, 28, 128, 8>;
+using Wide = Shape<16, 60, 128, 5>;
 
 // Calls f with the shape type and its TileCfg value for `cfg`.
 template <class S_, int CFG_>
@@ -85,6 +87,7 @@ template <class F>
 decltype(auto) with_shape(int cfg, F &&f) {
   if (cfg == kTile16x28) return f(ShapeTag<Small, kTile16x28>{});
   if (cfg == kTile20x28) return f(ShapeTag<Mid, kTile20x28>{});
+  if (cfg == kTile16x60) return f(ShapeTag<Wide, kTile16x60>{});
   return f(ShapeTag<Big, kTile32x60>{});
 }
 
@@ -245,6 +248,223 @@ __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields
   }
 }
 
+// Frame-count taper of a row or column at grid index g of an n-point axis,
+// for any g (points outside the grid clamp to the table's first entry; their
+// updates are masked out).
+__device__ __forceinline__ float axis_taper(const SimDesc &d, int g, int n) {
+  const int t = max(min(g + 1, n - g), 0);
+  return t < d.np ? __ldg(d.taper_tab + t) : 1.0f;
+}
+
+// A frame tile has no snapshot I/O this step, no injection term, and its own
+// columns lie inside the grid (its own rows may end at the grid's last row;
+// its halo may lie outside). It takes the vectorised path with per-point
+// taper factors and masks that keep points outside the updated region
+// 2 <= x < n-2 at their old values. (Injection tiles keep the one-column
+// path: there each thread adds the terms of at most a few points, whose
+// dependent loads of the plan and wavelet are the tile's critical path;
+// with two columns and four rows per thread that chain grew so long that
+// the source tile held back its neighbours' steps.)
+template <class S>
+__device__ __forceinline__ bool injection_tile(const SimDesc &d, int X0, int Z0) {
+  const InjPlan &p = d.plan;
+  return p.n && X0 < p.x0 + p.w && p.x0 < X0 + S::TX && Z0 < p.z0 + p.h && p.z0 < Z0 + S::TZ;
+}
+template <class S>
+__device__ __forceinline__ bool frame_tile(const SimDesc &d, int X0, int Z0, bool snap_io) {
+  return !snap_io && Z0 + S::TZ <= d.nz && !injection_tile<S>(d, X0, Z0);
+}
+
+__device__ __forceinline__ float2 lds2(const float *p) {
+  return *reinterpret_cast<const float2 *>(p);
+}
+__device__ __forceinline__ void sts2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
+
+// Phases B and C of the 60-column shapes (32 x 60, 16 x 60) with two z
+// columns per lane: every shared-memory access is a float2 (the z-direction
+// stencil of two adjacent points shares its loads), each warp walks
+// consecutive rows with the x-direction stencil values in registers, and the
+// difference coefficients are folded with 1/dx and 1/dz. Phase B: a warp
+// covers the 64 stress columns and RQ or RQ + 1 of the TX + 4 rows (32 x 60:
+// warps 0-3 five and 4-7 four of 36; 16 x 60: five each of 20); phase C:
+// lanes 0-29 cover the 60 own columns, each warp KV = TX / warps own rows.
+// FRAME false: an interior tile (taper exactly 1, every point updated);
+// FRAME true: a frame tile (taper = min of the row and column factors, which
+// is the table at the point's frame count because the Cerjan taper grows
+// with the count; points outside the updated region keep their values; own
+// rows beyond the grid's last row are skipped).
+// bb: this thread's buoyancy, rows X0 + KV w + k (KV = TX / warps own rows
+// per warp), columns Z0 + 2 lane + {0,1}.
+template <class S, bool ADJ, bool FRAME>
+__device__ __forceinline__ void tile_phases_v2(const SimDesc &d, const fast::Fields &out, int X0,
+                                               int Z0, const float (*VX)[S::W],
+                                               const float (*VZ)[S::W], float (*sxx_)[S::W],
+                                               float (*szz_)[S::W], float (*sxz_)[S::W],
+                                               const float (*slm)[S::W], const float (*smu)[S::W],
+                                               const float *bb) {
+  static_assert(S::TZ == 60, "two columns per lane over the 64 stress columns");
+  constexpr int TX = S::TX, TZ = S::TZ, WARPS = S::WARPS, SR = S::SR;
+  // Stress rows: warp w takes RQ or RQ + 1 consecutive rows; own rows: KV.
+  constexpr int RQ = SR / WARPS, RR = SR % WARPS, RB = RQ + (RR ? 1 : 0), KV = TX / WARPS;
+  static_assert(TX % WARPS == 0, "own rows split evenly over the warps");
+  const int ps = d.pitch, nx = d.nx, nz = d.nz;
+  const float dtv = ADJ ? -d.dt : d.dt;
+  const float c1x = (9.0f / 8.0f) * d.idx, c2x = (1.0f / 24.0f) * d.idx;
+  const float c1z = (9.0f / 8.0f) * d.idz, c2z = (1.0f / 24.0f) * d.idz;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  {
+    const int c = 2 + 2 * lane;  // box columns c, c + 1
+    const int gz = Z0 - 4 + c;
+    const bool z_own = c >= 4 && c < TZ + 4;
+    const int r0 = w * RQ + min(w, RR);
+    const int nr = RQ + (w < RR ? 1 : 0);
+    float tz0 = 1.0f, tz1 = 1.0f;
+    bool zi0 = true, zi1 = true;
+    if (FRAME) {
+      tz0 = axis_taper(d, gz, nz);
+      tz1 = axis_taper(d, gz + 1, nz);
+      zi0 = gz >= 2 && gz < nz - 2;
+      zi1 = gz + 1 >= 2 && gz + 1 < nz - 2;
+    }
+    float2 xm1 = lds2(&VX[r0 + 1][c]), x0 = lds2(&VX[r0 + 2][c]), xp1 = lds2(&VX[r0 + 3][c]),
+           xp2 = lds2(&VX[r0 + 4][c]);
+    float2 zm2 = lds2(&VZ[r0][c]), zm1 = lds2(&VZ[r0 + 1][c]), z0 = lds2(&VZ[r0 + 2][c]),
+           zp1 = lds2(&VZ[r0 + 3][c]);
+    int gp = (X0 - 2 + r0) * ps + gz;
+#pragma unroll
+    for (int k = 0; k < RB; ++k) {
+      if (k < nr) {
+        const int r = r0 + k, vr = r + 2;
+        const float2 lm = lds2(&slm[r][c]), mu = lds2(&smu[r][c]);
+        const float2 vxl = lds2(&VX[vr][c - 2]), vxr = lds2(&VX[vr][c + 2]);
+        const float2 vzl = lds2(&VZ[vr][c - 2]), vzr = lds2(&VZ[vr][c + 2]);
+        float2 sxx = lds2(&sxx_[r][c]), szz = lds2(&szz_[r][c]), sxz = lds2(&sxz_[r][c]);
+        const float ex0 = c1x * (xp1.x - x0.x) + c2x * (xm1.x - xp2.x);
+        const float ex1 = c1x * (xp1.y - x0.y) + c2x * (xm1.y - xp2.y);
+        const float ez0 = c1z * (z0.x - vzl.y) + c2z * (vzl.x - z0.y);
+        const float ez1 = c1z * (z0.y - z0.x) + c2z * (vzl.y - vzr.x);
+        const float g0 = (c1z * (x0.y - x0.x) + c2z * (vxl.y - vxr.x)) +
+                         (c1x * (z0.x - zm1.x) + c2x * (zm2.x - zp1.x));
+        const float g1 = (c1z * (vxr.x - x0.y) + c2z * (x0.x - vxr.y)) +
+                         (c1x * (z0.y - zm1.y) + c2x * (zm2.y - zp1.y));
+        const float la0 = lm.x - 2.0f * mu.x, la1 = lm.y - 2.0f * mu.y;
+        float nxx0 = sxx.x + dtv * (lm.x * ex0 + la0 * ez0);
+        float nxx1 = sxx.y + dtv * (lm.y * ex1 + la1 * ez1);
+        float nzz0 = szz.x + dtv * (la0 * ex0 + lm.x * ez0);
+        float nzz1 = szz.y + dtv * (la1 * ex1 + lm.y * ez1);
+        float nxz0 = sxz.x + dtv * mu.x * g0;
+        float nxz1 = sxz.y + dtv * mu.y * g1;
+        if (FRAME) {
+          const int gx = X0 - 2 + r;
+          const bool xi = gx >= 2 && gx < nx - 2;
+          const float tr = axis_taper(d, gx, nx);
+          const float t0 = fminf(tz0, tr), t1 = fminf(tz1, tr);
+          const bool u0 = xi && zi0, u1 = xi && zi1;
+          sxx.x = u0 ? t0 * nxx0 : sxx.x;
+          szz.x = u0 ? t0 * nzz0 : szz.x;
+          sxz.x = u0 ? t0 * nxz0 : sxz.x;
+          sxx.y = u1 ? t1 * nxx1 : sxx.y;
+          szz.y = u1 ? t1 * nzz1 : szz.y;
+          sxz.y = u1 ? t1 * nxz1 : sxz.y;
+        } else {
+          sxx = make_float2(nxx0, nxx1);
+          szz = make_float2(nzz0, nzz1);
+          sxz = make_float2(nxz0, nxz1);
+        }
+        sts2(&sxx_[r][c], sxx);
+        sts2(&szz_[r][c], szz);
+        sts2(&sxz_[r][c], sxz);
+        if (z_own && r >= 2 && r < TX + 2 && (!FRAME || X0 - 2 + r < nx)) {
+          sts2(out.txx + gp, sxx);
+          sts2(out.tzz + gp, szz);
+          sts2(out.txz + gp, sxz);
+        }
+        gp += ps;
+        if (k + 1 < nr) {
+          xm1 = x0;
+          x0 = xp1;
+          xp1 = xp2;
+          xp2 = lds2(&VX[vr + 3][c]);
+          zm2 = zm1;
+          zm1 = z0;
+          z0 = zp1;
+          zp1 = lds2(&VZ[vr + 2][c]);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (lane < TZ / 2) {
+    const float(*TXX)[S::W] = sxx_;
+    const float(*TZZ)[S::W] = szz_;
+    const float(*TXZ)[S::W] = sxz_;
+    const int cc = 4 + 2 * lane;  // box columns cc, cc + 1
+    const int gz = Z0 + 2 * lane;
+    const int lx0 = KV * w;
+    const int s0 = lx0 + 2;  // stress box row of the first point
+    float tz0 = 1.0f, tz1 = 1.0f;
+    bool zi0 = true, zi1 = true;
+    if (FRAME) {
+      tz0 = axis_taper(d, gz, nz);
+      tz1 = axis_taper(d, gz + 1, nz);
+      zi0 = gz >= 2 && gz < nz - 2;
+      zi1 = gz + 1 >= 2 && gz + 1 < nz - 2;
+    }
+    float2 am2 = lds2(&TXX[s0 - 2][cc]), am1 = lds2(&TXX[s0 - 1][cc]), a0 = lds2(&TXX[s0][cc]),
+           ap1 = lds2(&TXX[s0 + 1][cc]);
+    float2 bm1 = lds2(&TXZ[s0 - 1][cc]), b0 = lds2(&TXZ[s0][cc]), bp1 = lds2(&TXZ[s0 + 1][cc]),
+           bp2 = lds2(&TXZ[s0 + 2][cc]);
+    int gq = (X0 + lx0) * ps + gz;
+#pragma unroll
+    for (int k = 0; k < KV; ++k) {
+      const int r = s0 + k, lx = lx0 + k;
+      if (FRAME && X0 + lx >= nx) break;  // uniform per warp: rows past the grid's last
+      const float2 txzl = lds2(&TXZ[r][cc - 2]), txzr = lds2(&TXZ[r][cc + 2]);
+      const float2 tzzl = lds2(&TZZ[r][cc - 2]), tzz0 = lds2(&TZZ[r][cc]),
+                   tzzr = lds2(&TZZ[r][cc + 2]);
+      const float ax0 = (c1x * (a0.x - am1.x) + c2x * (am2.x - ap1.x)) +
+                        (c1z * (b0.x - txzl.y) + c2z * (txzl.x - b0.y));
+      const float ax1 = (c1x * (a0.y - am1.y) + c2x * (am2.y - ap1.y)) +
+                        (c1z * (b0.y - b0.x) + c2z * (txzl.y - txzr.x));
+      const float az0 = (c1x * (bp1.x - b0.x) + c2x * (bm1.x - bp2.x)) +
+                        (c1z * (tzz0.y - tzz0.x) + c2z * (tzzl.y - tzzr.x));
+      const float az1 = (c1x * (bp1.y - b0.y) + c2x * (bm1.y - bp2.y)) +
+                        (c1z * (tzzr.x - tzz0.y) + c2z * (tzz0.x - tzzr.y));
+      float2 vx = lds2(&VX[lx + 4][cc]), vz = lds2(&VZ[lx + 4][cc]);
+      const float bdt0 = bb[2 * k] * dtv, bdt1 = bb[2 * k + 1] * dtv;
+      const float nvx0 = vx.x + bdt0 * ax0, nvx1 = vx.y + bdt1 * ax1;
+      const float nvz0 = vz.x + bdt0 * az0, nvz1 = vz.y + bdt1 * az1;
+      if (FRAME) {
+        const int gx = X0 + lx;
+        const bool xi = gx >= 2 && gx < nx - 2;
+        const float tr = axis_taper(d, gx, nx);
+        const float t0 = fminf(tz0, tr), t1 = fminf(tz1, tr);
+        const bool u0 = xi && zi0, u1 = xi && zi1;
+        vx.x = u0 ? t0 * nvx0 : vx.x;
+        vz.x = u0 ? t0 * nvz0 : vz.x;
+        vx.y = u1 ? t1 * nvx1 : vx.y;
+        vz.y = u1 ? t1 * nvz1 : vz.y;
+      } else {
+        vx = make_float2(nvx0, nvx1);
+        vz = make_float2(nvz0, nvz1);
+      }
+      sts2(out.vx + gq, vx);
+      sts2(out.vz + gq, vz);
+      gq += ps;
+      if (k + 1 < KV) {
+        am2 = am1;
+        am1 = a0;
+        a0 = ap1;
+        ap1 = lds2(&TXX[r + 2][cc]);
+        bm1 = b0;
+        b0 = bp1;
+        bp1 = bp2;
+        bp2 = lds2(&TXZ[r + 3][cc]);
+      }
+    }
+  }
+}
+
 // One tile's time step. `maps` are the tensor maps of this step's input set;
 // the kernels below pass them either as a kernel parameter (single model:
 // the copies can be issued without waiting for any load) or from the
@@ -290,6 +510,11 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   const bool snap_io = (it % d.si) == 0 && d.accu[0] != nullptr && (ADJ || store);
   const size_t soff = (size_t)(it / d.si) * nx * nz;
   const bool inner = interior_tile<S>(d, X0, Z0, snap_io);
+  // The 60-column shapes take the vectorised path on interior and frame
+  // tiles; the 28-column shapes keep the one-column paths (interior and
+  // taper).
+  constexpr bool V2 = S::TZ == 60;
+  const bool frame = V2 && !inner && frame_tile<S>(d, X0, Z0, snap_io);
   const bool tapered = TAPERED && !inner && taper_tile<S>(d, X0, Z0, snap_io);
 
   // This thread's buoyancy values for phase C (the medium does not change
@@ -302,10 +527,25 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   const int gzc = Z0 + lzc;
   const bool col_ok = lzc < TZ && gzc < nz;
   float bb[KC];
+  if (V2 && (inner || frame)) {
+    // Two columns per lane (lanes 0-29), rows X0 + KV w + k: own points (the
+    // columns inside the grid; rows past its last row read nothing).
+    constexpr int KV = TX / S::WARPS;
+    static_assert(!V2 || KC == 2 * KV, "KV rows of two columns per thread");
 #pragma unroll
-  for (int k = 0; k < KC; ++k) {
-    const int gx = (inner || tapered) ? X0 + q * KC + k : X0 + q + G * k;
-    bb[k] = (col_ok && gx < nx) ? __ldg(d.b + gx * ps + gzc) : 0.f;
+    for (int k = 0; k < KV; ++k) {
+      float2 v = make_float2(0.f, 0.f);
+      if (lane < TZ / 2 && X0 + KV * w + k < nx)
+        v = __ldg(reinterpret_cast<const float2 *>(d.b + (X0 + KV * w + k) * ps + Z0 + 2 * lane));
+      bb[2 * k] = v.x;
+      bb[2 * k + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+      const int gx = (inner || tapered) ? X0 + q * KC + k : X0 + q + G * k;
+      bb[k] = (col_ok && gx < nx) ? __ldg(d.b + gx * ps + gzc) : 0.f;
+    }
   }
   griddep_wait();
   // (sync_copy false: the caller has just passed a barrier that follows
@@ -368,9 +608,20 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   const float(*VX)[W] = sv[0];
   const float(*VZ)[W] = sv1;
 
-  if (inner) {
-    tile_phases<S, ADJ, false>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
-    return true;
+  if constexpr (V2) {
+    if (inner) {
+      tile_phases_v2<S, ADJ, false>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
+      return true;
+    }
+    if (frame) {
+      tile_phases_v2<S, ADJ, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
+      return true;
+    }
+  } else {
+    if (inner) {
+      tile_phases<S, ADJ, false>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
+      return true;
+    }
   }
   if (TAPERED && tapered) {
     tile_phases<S, ADJ, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
@@ -481,7 +732,7 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
 // Single simulation: tensor maps as a parameter, tiles from blockIdx
 // (row-major over tiles_z tile columns).
 template <class S, int CFG, bool ADJ>
-__global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
+__global__ void __launch_bounds__(S::NT, S::MINB)
     fused_step_tma(const __grid_constant__ SimDesc d, int tiles_z, int it, int parity, int store,
                    int *err) {
   const int bx = blockIdx.x, tx = bx / tiles_z, tz = bx - tx * tiles_z;
@@ -492,7 +743,7 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
 // Many simulations: tile table entries (sim, x0, z0, first) per CTA. With
 // `active` non-null, the CTAs of simulations whose flag is 0 return at once.
 template <class S, int CFG, bool ADJ>
-__global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
+__global__ void __launch_bounds__(S::NT, S::MINB)
     fused_step_tma_batch(const SimDesc *__restrict__ sims, const int4 *__restrict__ tiles,
                          const int *__restrict__ active, int it, int parity, int store, int *err) {
   const int4 t = tiles[blockIdx.x];
@@ -529,7 +780,7 @@ __device__ __forceinline__ bool wait_at_least(const unsigned *p, unsigned v) {
 // is cumulative, so it orders every store of the CTA that precedes the
 // barrier, and the waiting side's ld.acquire.gpu sees them all.
 template <class S, int CFG, bool ADJ>
-__global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
+__global__ void __launch_bounds__(S::NT, S::MINB)
     fused_steps_tma(const __grid_constant__ SimDesc d, int tiles_x, int tiles_z, int it0,
                     int n_steps, int parity0, int store, int *err, unsigned *sched) {
   __shared__ int s_item;
@@ -608,7 +859,7 @@ __global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
 // publication as fused_steps_tma; inactive simulations' items are skipped
 // (their neighbours are inactive too).
 template <class S, int CFG>
-__global__ void __launch_bounds__(S::NT, (S::NT == 256 ? 3 : 8))
+__global__ void __launch_bounds__(S::NT, S::MINB)
     fused_steps_tma_batch(const SimDesc *__restrict__ sims, const int4 *__restrict__ tiles,
                           const int *__restrict__ active, int n_tiles, int n_steps, int store,
                           int *err, unsigned *sched) {

@@ -535,7 +535,7 @@ class fdModel:
     def kernel_variant(self, name):
         _capi.check(self._lib.psv_set_kernel_variant(self._h, self.VARIANTS[name]))
 
-    TILE_SHAPES = {"32x60": 0, "16x28": 1, "20x28": 2}
+    TILE_SHAPES = {"32x60": 0, "16x28": 1, "20x28": 2, "16x60": 3}
 
     @property
     def tile_shape(self):

@@ -20,7 +20,7 @@ def small_models(n=3, nt=300):
     return models
 
 
-@pytest.mark.parametrize("shape", ["16x28", "20x28", "32x60"])
+@pytest.mark.parametrize("shape", ["16x28", "20x28", "32x60", "16x60"])
 @pytest.mark.parametrize("persistent", [True, False])
 def test_batch_matches_individual_runs(shape, persistent):
     models = small_models()
@@ -69,7 +69,7 @@ def test_batch_autotune_picks_a_shape():
     b = psv.Batch()
     for m in models:
         b.add_all_shots(m)
-    assert b.autotune(20) in ("32x60", "16x28", "20x28")
+    assert b.autotune(20) in ("32x60", "16x28", "20x28", "16x60")
 
 
 @pytest.mark.parametrize("persistent", [True, False])

@@ -67,11 +67,14 @@ def test_c1_fp32_default_scheme_vs_fp64_full_run():
         assert e <= FP32_TOL, errs
 
 
-@pytest.mark.parametrize("variant", ["fused_tma_persistent", "fused_tma"])
-def test_c1_fp32_wavefields_vs_fp64_while_wave_in_grid(variant):
+@pytest.mark.parametrize("variant,shape", [("fused_tma_persistent", "32x60"),
+                                           ("fused_tma_persistent", "16x60"),
+                                           ("fused_tma", "32x60")])
+def test_c1_fp32_wavefields_vs_fp64_while_wave_in_grid(variant, shape):
     nt = 1500
     m32 = workloads.c1_model(nt=nt)
     m32.kernel_variant = variant
+    m32.tile_shape = shape
     m32.forward_simulate(0, False)
     m64 = workloads.c1_model(nt=nt, precision="fp64")
     m64.forward_simulate(0, False)

@@ -230,7 +230,7 @@ def test_tile_shapes_agree_and_autotune(golden):
     rounding and stay within tolerance of the reference; the autotuner picks
     one of them."""
     res = {}
-    for shape in ("32x60", "16x28", "20x28"):
+    for shape in ("32x60", "16x28", "20x28", "16x60"):
         m = psv.fdModel(SMALL_INI, precision="fp32")
         m.tile_shape = shape
         assert m.tile_shape == shape
@@ -242,11 +242,12 @@ def test_tile_shapes_agree_and_autotune(golden):
     for name in ("rtf_ux", "rtf_uz"):
         assert rel_l2(res["32x60"][name], res["16x28"][name]) <= 1e-5
         assert rel_l2(res["32x60"][name], res["20x28"][name]) <= 1e-5
+        assert rel_l2(res["32x60"][name], res["16x60"][name]) <= 1e-5
     m = psv.fdModel(SMALL_INI, precision="fp32")
-    assert m.autotune(20) in ("32x60", "16x28", "20x28")
+    assert m.autotune(20) in ("32x60", "16x28", "20x28", "16x60")
 
 
-@pytest.mark.parametrize("shape", ["32x60", "16x28", "20x28"])
+@pytest.mark.parametrize("shape", ["32x60", "16x28", "20x28", "16x60"])
 @pytest.mark.parametrize("ini", [SMALL_INI, NB2_INI])
 def test_persistent_step_matches_per_step_launches_bitwise(golden, shape, ini):
     """The persistent variant runs the per-step variant's arithmetic tile by
