@@ -215,7 +215,7 @@ def fwi_gradients(steps, warmup, with_cpu):
     return out
 
 
-def fwi_gradients_c3(steps):
+def fwi_gradients_c3(steps, with_cpu=False):
     """FWI gradients/s on the differentiation workload (1000 x 400 inner
     cells, 8 shots, nt = 6000, FP32 wave fields, FP64 kernel sums): the
     gradient of the L2 misfit through the torch.autograd layer, as the exact
@@ -262,7 +262,37 @@ def fwi_gradients_c3(steps):
             res["device_bytes"] = m.exact_bytes(kw["checkpoint_every"])
         out[name] = res
     out["value"] = out["checkpoint_100"]["value"]
+    if with_cpu:
+        out["cpu_baseline"] = cpu_baseline_c3()
     return out
+
+
+def cpu_baseline_c3(n_steps=600):
+    """The oracle port (C, OpenMP, all host threads) on a bounded sample of
+    the differentiation workload: the reference's gradient (run_model:
+    forward with snapshots every 10 steps, misfit, adjoint sources, adjoint
+    with kernel correlation, velocity kernels) of one shot over n_steps
+    steps on the full 1100 x 500 grid, scaled to a full gradient (8 shots x
+    6000 steps)."""
+    from oracle import portbind
+    from psvwave_gb300 import workloads
+
+    p = workloads.c3_params(nt=n_steps, n_shots=1)
+    true, start = workloads.c3_media(workloads.c3_params())
+    o = portbind.OracleModel(params=p)
+    o.set_parameter_fields(*true)
+    o.forward_simulate(0, False)
+    o.set_observed_data(*o.get_synthetic_data())
+    o.set_parameter_fields(*start)
+    t0 = time.perf_counter()
+    o.run_model(True)
+    t = time.perf_counter() - t0
+    full = t * 8 * (6000 / n_steps)
+    return {"value": 1.0 / full, "unit": "FWI gradients/s",
+            "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)), "kind": "port",
+            "sample": "oracle port run_model (reference adjoint kernels), 1 shot x %d steps on "
+                      "the c3 grid in %.2f s, scaled x8 shots x%g steps" % (n_steps, t,
+                                                                       6000 / n_steps)}
 
 
 def mc_samples_c4():
@@ -281,16 +311,24 @@ def mc_samples_c4():
     return out
 
 
-def batched(steps, warmup):
+def batched(steps, warmup, rank=0, world=1, with_cpu=False):
     """Aggregate Gcell-updates/s of the batching workload (256 models of
     uneven sizes, 1-4 shots each, nt = 1000): all shots of all models in one
     launch per time step (one CUDA graph), versus the same models run one
-    after another, each shot its own forward_simulate."""
+    after another, each shot its own forward_simulate. Under torchrun the
+    models are split round-robin across the ranks (model k on rank
+    k % world, psvwave_gb300.distributed.shard), each rank advancing its
+    share in one batch; the rate is the whole set's cell-updates over the
+    slowest rank's time (a fixed workload: strong scaling)."""
     import psvwave_gb300 as psv
     from psvwave_gb300 import workloads
+    from psvwave_gb300.distributed import shard
 
+    pairs = workloads.c2_models()
+    mine = shard(len(pairs), rank, world)
     models = []
-    for p, media in workloads.c2_models():
+    for k in mine:
+        p, media = pairs[k]
         m = psv.fdModel.from_parameters(p)
         m.set_parameter_fields(*media)
         models.append(m)
@@ -304,10 +342,29 @@ def batched(steps, warmup):
         b.forward()
     b_times = []
     for _ in range(steps):
+        if world > 1:
+            import torch
+            torch.distributed.barrier()
         t0 = time.perf_counter()
         b.forward()
         b_times.append(time.perf_counter() - t0)
-    batched_rate = info["cells"] * nt / (sum(b_times) / len(b_times)) / 1e9
+    mean_t = sum(b_times) / len(b_times)
+    cells = info["cells"]
+    if world > 1:
+        import torch
+        t = torch.tensor([mean_t, cells], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        mean_t, cells = float(t[0]), float(t[1])
+    batched_rate = cells * nt / mean_t / 1e9
+    out = {"value": batched_rate, "unit": "Gcell-updates/s",
+           "workload": "c2: 256 seeded models, nx_inner U[200,800], nz_inner U[100,400], "
+                       "25-cell boundary, 1-4 shots, Ricker 20-50 Hz, nt=1000, forward only",
+           "members": info["members"], "cells_per_step": cells, "tiles": info["tiles"],
+           "tile_shape": shape, "persistent": b.persistent}
+    if world > 1:
+        out["parallelism"] = "models round-robin over %d ranks, no collective on the data path" % world
+        return out
     for m in models:  # warm the per-model graphs
         for _ in range(2):
             for s_ in range(m.n_shots):
@@ -317,13 +374,36 @@ def batched(steps, warmup):
         for s_ in range(m.n_shots):
             m.forward_simulate(s_, False)
     seq = time.perf_counter() - t0
-    seq_rate = info["cells"] * nt / seq / 1e9
-    return {"value": batched_rate, "unit": "Gcell-updates/s",
-            "workload": "c2: 256 seeded models, nx_inner U[200,800], nz_inner U[100,400], "
-                        "25-cell boundary, 1-4 shots, Ricker 20-50 Hz, nt=1000, forward only",
-            "members": info["members"], "cells_per_step": info["cells"], "tiles": info["tiles"],
-            "tile_shape": shape, "one_launch_per_model": seq_rate,
-            "speedup_vs_one_launch_per_model": batched_rate / seq_rate}
+    seq_rate = cells * nt / seq / 1e9
+    out["one_launch_per_model"] = seq_rate
+    out["speedup_vs_one_launch_per_model"] = batched_rate / seq_rate
+    if with_cpu:
+        out["cpu_baseline"] = cpu_baseline_c2(pairs)
+    return out
+
+
+def cpu_baseline_c2(pairs, n_models=4, n_steps=200):
+    """The oracle port (C, OpenMP, all host threads) on a bounded sample of
+    the batching workload: every shot of the first n_models models, n_steps
+    of their 1000 time steps, in Gcell-updates/s."""
+    from oracle import portbind
+
+    cells = 0.0
+    t = 0.0
+    for p, media in pairs[:n_models]:
+        q = dict(p)
+        q.update(nt=n_steps, snapshot_interval=n_steps)
+        o = portbind.OracleModel(params=q)
+        o.set_parameter_fields(*media)
+        t0 = time.perf_counter()
+        for s_ in range(o.n_shots):
+            o.forward_simulate(s_, False)
+        t += time.perf_counter() - t0
+        cells += float(o.nx * o.nz) * n_steps * o.n_shots
+    return {"value": cells / t / 1e9, "unit": "Gcell-updates/s",
+            "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)), "kind": "port",
+            "sample": "oracle port forward, every shot of the first %d c2 models, %d of 1000 "
+                      "steps, %.1f s" % (n_models, n_steps, t)}
 
 
 def run_reference(args):
@@ -544,12 +624,15 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(workloads.c1_params, media, moment=workloads.c1_moment())
     secondary = None
-    if rank == 0 and not args.no_secondary:
-        secondary = {"fwi_gradients": fwi_gradients(args.steps, args.warmup,
-                                                    world == 1 and not args.no_cpu_baseline),
-                     "batched": batched(args.steps, args.warmup),
-                     "fwi_gradients_c3": fwi_gradients_c3(min(args.steps, 2)),
-                     "mc_samples_c4": mc_samples_c4()}
+    if not args.no_secondary:
+        with_cpu = world == 1 and not args.no_cpu_baseline
+        # Every rank takes its share of the c2 models; the rest runs on rank 0.
+        sharded = batched(args.steps, args.warmup, rank, world, with_cpu)
+        if rank == 0:
+            secondary = {"fwi_gradients": fwi_gradients(args.steps, args.warmup, with_cpu),
+                         "batched": sharded,
+                         "fwi_gradients_c3": fwi_gradients_c3(min(args.steps, 2), with_cpu),
+                         "mc_samples_c4": mc_samples_c4()}
 
     if rank == 0:
         line = {

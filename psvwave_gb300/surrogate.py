@@ -396,7 +396,8 @@ def _surrogate_ug(net, z, s2, screen=1.0, force=1.0):
     return u, (force / s2) * g + z
 
 
-def da_hmc(post, net, z0, n_iter, eps, n_leap, seed=0, record=True, screen=1.0, force=1.0):
+def da_hmc(post, net, z0, n_iter, eps, n_leap, seed=0, record=True, screen=1.0, force=1.0,
+           chains=None):
     """Delayed-acceptance HMC of len(z0) chains in parallel. Returns a dict
     with the samples [n_iter][B][...], acceptance counts and timings.
 
@@ -406,20 +407,42 @@ def da_hmc(post, net, z0, n_iter, eps, n_leap, seed=0, record=True, screen=1.0, 
     per iteration). Any screen and force weights leave the posterior exact:
     leapfrog with any force is volume-preserving and reversible, and the
     second stage divides out the first stage's density. screen = force = 0
-    screens with the prior alone."""
+    screens with the prior alone.
+
+    chains = (indices, n_total): z0 holds chains `indices` of a run of
+    n_total chains. The random numbers of all n_total chains are drawn from
+    `seed` and these chains use their share, so each chain follows the same
+    trajectory as in the full run (the chains of a run can be split across
+    processes)."""
     gen = torch.Generator(device=z0.device)
     gen.manual_seed(seed)
     rng = np.random.default_rng(seed)
     s2 = post.s2
     z = z0.clone().float()
     B = z.shape[0]
+    if chains is None:
+        sel_idx, n_total = None, B
+    else:
+        sel_idx, n_total = np.asarray(chains[0], dtype=np.int64), int(chains[1])
+        if sel_idx.size != B:
+            raise ValueError("chains must list one index per row of z0")
+    sel_t = None if sel_idx is None else torch.tensor(sel_idx, device=z.device)
+
+    def draw_p():
+        p = torch.randn((n_total,) + tuple(z.shape[1:]), generator=gen, device=z.device)
+        return p if sel_t is None else p[sel_t]
+
+    def draw_u():
+        u = rng.random(n_total)
+        return u if sel_idx is None else u[sel_idx]
+
     U = post.potentials(z)
     Ut, gt = _surrogate_ug(net, z, s2, screen, force)
     samples = [] if record else None
     stage1 = stage2 = proposals = 0
     t0 = time.perf_counter()
     for _ in range(n_iter):
-        p = torch.randn(z.shape, generator=gen, device=z.device)
+        p = draw_p()
         k0 = 0.5 * (p.double() ** 2).reshape(B, -1).sum(1)
         zq, pq = z.clone(), p - 0.5 * eps * gt
         for l in range(n_leap):
@@ -431,11 +454,11 @@ def da_hmc(post, net, z0, n_iter, eps, n_leap, seed=0, record=True, screen=1.0, 
         h1 = (Uq + k1).cpu().numpy()
         finite = np.isfinite(h1) & np.isfinite(h0)
         with np.errstate(over="ignore", invalid="ignore"):
-            a1 = finite & (np.log(rng.random(B)) < np.where(finite, h0 - h1, -np.inf))
+            a1 = finite & (np.log(draw_u()) < np.where(finite, h0 - h1, -np.inf))
         # The judge: one batched forward of the proposals that passed.
         Uy = post.potentials(zq, a1)
         ut_x, ut_y = Ut.cpu().numpy(), Uq.cpu().numpy()
-        u2 = np.log(rng.random(B))
+        u2 = np.log(draw_u())
         with np.errstate(over="ignore", invalid="ignore"):
             a2 = a1 & (u2 < np.where(a1, -(Uy - U) + (ut_y - ut_x), -np.inf))
         acc = a2
