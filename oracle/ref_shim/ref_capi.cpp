@@ -133,6 +133,12 @@ void ref_set_data(void *h, int observed, const double *ux, const double *uz) {
 void ref_forward(void *h, int shot, int store) {  // src/fdModel.cpp:526
   static_cast<fdModel *>(h)->forward_simulate(shot, store != 0, false, false);
 }
+// The same with the reference's wave-field dumps (snapshots/vx%05d.txt and
+// vz%05d.txt every 10 steps, relative to the working directory,
+// src/fdModel.cpp:753-776).
+void ref_forward_output(void *h, int shot, int store) {
+  static_cast<fdModel *>(h)->forward_simulate(shot, store != 0, false, true);
+}
 void ref_adjoint(void *h, int shot) {  // src/fdModel.cpp:789
   static_cast<fdModel *>(h)->adjoint_simulate(shot, false);
 }

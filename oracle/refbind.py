@@ -46,6 +46,7 @@ def _load():
         lib.ref_set_parameter_fields.argtypes = [vp, dp, dp, dp]
         lib.ref_set_data.argtypes = [vp, ctypes.c_int, dp, dp]
         lib.ref_forward.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+        lib.ref_forward_output.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         lib.ref_adjoint.argtypes = [vp, ctypes.c_int]
         lib.ref_misfit.restype = ctypes.c_double
         lib.ref_misfit.argtypes = [vp]
@@ -183,3 +184,34 @@ class RefModel:
 
     def get_synthetic_data(self):
         return self.array("rtf_ux"), self.array("rtf_uz")
+
+    def get_observed_data(self):
+        return self.array("rtf_ux_true"), self.array("rtf_uz_true")
+
+    def forward_simulate_output(self, shot, store_fields=True):
+        """forward_simulate with the reference's wave-field dumps into
+        snapshots/ under the working directory."""
+        _load().ref_forward_output(self._h, shot, int(store_fields))
+
+    def write_receivers(self):
+        _load().ref_write_receivers(self._h)
+
+    def write_sources(self):
+        _load().ref_write_sources(self._h)
+
+    def write_kernels(self):
+        _load().ref_write_kernels(self._h)
+
+    def load_receivers(self):
+        """The reference's load_receivers (observed data from
+        observed_data_folder/rtf_u{x,z}{shot}.txt); raises on its errors."""
+        if _load().ref_load_receivers(self._h) != 0:
+            raise ValueError(_load().ref_last_error().decode())
+
+    def load_vector(self, path):
+        """The reference's load_vector: 3 nx_free nz_free values, one per
+        free cell and parameter (not per basis block)."""
+        out = np.empty(3 * self.info["nx_free_parameters"] * self.info["nz_free_parameters"])
+        if _load().ref_load_vector(self._h, str(path).encode(), _dp(out)) != 0:
+            raise ValueError(_load().ref_last_error().decode())
+        return out
