@@ -28,7 +28,11 @@
 // lo: about 48 significant bits, like the FP64 sums of exact_step_tile, but
 // on the FP32 pipes (GB300 issues FP64 at a small fraction of the FP32
 // rate, and FP64 sums were most of this kernel's time). finish() turns the
-// pairs into FP64 once per gradient.
+// pairs into FP64 once per gradient. With Step::g_part set, each step's
+// terms first go into an FP32 partial sum per point (one float4 for lm, la,
+// mu, b), which the flush steps (every few steps, and the last) add into
+// the pairs: per step the kernel then reads and writes 16 bytes of sums per
+// point instead of 32 (the pairs' traffic on flush steps only).
 //
 // Tiles whose 4-halo region lies inside the updated region and at least np
 // frames deep (taper exactly 1) and that hold no source point take a path
@@ -100,7 +104,8 @@ __device__ __forceinline__ float2 ff_add(float2 a, float x) {
 template <bool INNER>
 __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int Z0,
                                           const float2 *glm, const float2 *gla,
-                                          const float2 *gmu, const float2 *gb) {
+                                          const float2 *gmu, const float2 *gb,
+                                          const float4 *gpart) {
   const int tid = threadIdx.x, lane = tid & 31, wr = tid >> 5;
   const int iz = Z0 + lane;
   const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
@@ -213,22 +218,34 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
     a.olv[0][p] = ovx;
     a.olv[1][p] = ovz;
     float2 g_b = gb[j];
+    // With partial sums (a.g_part): this step's terms go into the FP32
+    // partial of the point (lm, la, mu, b); on a flush step the partial plus
+    // the terms go into the float-float pairs and the partial restarts at 0.
+    const bool part = a.g_part != nullptr;
+    float4 gq = gpart[j];
+    float t_lm = 0.f, t_la = 0.f, t_mu = 0.f, t_b = 0.f;
     if (in) {
       // grad_b += dt T lv . A tau^{n+1}
       const float ax = (c1 * (FXX[s] - FXX[s - W]) + c2 * (FXX[s - 2 * W] - FXX[s + W])) * a.idx +
                        (c1 * (FXZ[s] - FXZ[s - 1]) + c2 * (FXZ[s - 2] - FXZ[s + 1])) * a.idz;
       const float az = (c1 * (FXZ[s + W] - FXZ[s]) + c2 * (FXZ[s - W] - FXZ[s + 2 * W])) * a.idx +
                        (c1 * (FZZ[s + 1] - FZZ[s]) + c2 * (FZZ[s - 1] - FZZ[s + 2])) * a.idz;
-      g_b = ff_add(g_b, (a.dt * tp) * (lvx * ax + lvz * az));
+      t_b = (a.dt * tp) * (lvx * ax + lvz * az);
+      if (!part) g_b = ff_add(g_b, t_b);
       // Medium gradients from the strain rates of v^n.
       const float ex = (c1 * (FVX[s + W] - FVX[s]) + c2 * (FVX[s - W] - FVX[s + 2 * W])) * a.idx;
       const float ez = (c1 * (FVZ[s] - FVZ[s - 1]) + c2 * (FVZ[s - 2] - FVZ[s + 1])) * a.idz;
       const float gxz = (c1 * (FVX[s + 1] - FVX[s]) + c2 * (FVX[s - 1] - FVX[s + 2])) * a.idz +
                         (c1 * (FVZ[s] - FVZ[s - W]) + c2 * (FVZ[s - 2 * W] - FVZ[s + W])) * a.idx;
       const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
-      a.g_lm[u] = ff_add(glm[j], a.dt * (yxx * ex + yzz * ez));
-      a.g_la[u] = ff_add(gla[j], a.dt * (yxx * ez + yzz * ex));
-      a.g_mu[u] = ff_add(gmu[j], a.dt * yxz * gxz);
+      t_lm = a.dt * (yxx * ex + yzz * ez);
+      t_la = a.dt * (yxx * ez + yzz * ex);
+      t_mu = a.dt * yxz * gxz;
+      if (!part) {
+        a.g_lm[u] = ff_add(glm[j], t_lm);
+        a.g_la[u] = ff_add(gla[j], t_la);
+        a.g_mu[u] = ff_add(gmu[j], t_mu);
+      }
     }
     // Source terms s = coef stf dt b / div at their points depend on b.
     const InjPlan &pl = a.plan;
@@ -239,15 +256,35 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
         const InjTerm t = pl.terms[k];
         if (t.kind != 0) continue;
         const double ds = ((t.coef * a.stf[(size_t)t.index * a.nt + a.it]) * a.dt_d) / t.div;
-        g_b = ff_add(g_b, (float)(ds * (double)(t.field == 0 ? lvx : lvz)));
+        const float ts = (float)(ds * (double)(t.field == 0 ? lvx : lvz));
+        if (part)
+          t_b += ts;
+        else
+          g_b = ff_add(g_b, ts);
         src = true;
       }
     }
-    if (in || src) a.g_b[u] = g_b;
+    if (!part) {
+      if (in || src) a.g_b[u] = g_b;
+      continue;
+    }
+    gq.x += t_lm;
+    gq.y += t_la;
+    gq.z += t_mu;
+    gq.w += t_b;
+    if (a.flush) {
+      a.g_lm[u] = ff_add(glm[j], gq.x);
+      a.g_la[u] = ff_add(gla[j], gq.y);
+      a.g_mu[u] = ff_add(gmu[j], gq.z);
+      a.g_b[u] = ff_add(g_b, gq.w);
+      a.g_part[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else if (in || src) {
+      a.g_part[u] = gq;
+    }
   }
 }
 
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, 4)
     exact_step_tma(const __grid_constant__ Maps maps, const Step a, int tiles_z) {
   extern __shared__ unsigned char smem_raw[];
   float *sm = reinterpret_cast<float *>(
@@ -287,17 +324,24 @@ __global__ void __launch_bounds__(NT)
   // gradient sums, loaded while the copies fly.
   const int lane = tid & 31, wr = tid >> 5;
   const int iz = Z0 + lane;
+  // (With partial sums, the pairs are read only on flush steps.)
   float2 glm[ROWS], gla[ROWS], gmu[ROWS], gb[ROWS];
+  float4 gpart[ROWS];
+  const bool pairs = a.g_part == nullptr || a.flush;
 #pragma unroll
   for (int j = 0; j < ROWS; ++j) {
     const int ix = X0 + wr + j * (NT / 32);
     glm[j] = gla[j] = gmu[j] = gb[j] = make_float2(0.f, 0.f);
+    gpart[j] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ix < a.nx && iz < a.nz) {
       const size_t u = (size_t)ix * a.nz + iz;
-      glm[j] = a.g_lm[u];
-      gla[j] = a.g_la[u];
-      gmu[j] = a.g_mu[u];
-      gb[j] = a.g_b[u];
+      if (pairs) {
+        glm[j] = a.g_lm[u];
+        gla[j] = a.g_la[u];
+        gmu[j] = a.g_mu[u];
+        gb[j] = a.g_b[u];
+      }
+      if (a.g_part) gpart[j] = a.g_part[u];
     }
   }
 
@@ -318,9 +362,9 @@ __global__ void __launch_bounds__(NT)
                      !(pl.n && X0 < pl.x0 + pl.w && pl.x0 < X0 + TX && Z0 < pl.z0 + pl.h &&
                        pl.z0 < Z0 + TZ);
   if (inner)
-    tile_body<true>(a, sm, X0, Z0, glm, gla, gmu, gb);
+    tile_body<true>(a, sm, X0, Z0, glm, gla, gmu, gb, gpart);
   else
-    tile_body<false>(a, sm, X0, Z0, glm, gla, gmu, gb);
+    tile_body<false>(a, sm, X0, Z0, glm, gla, gmu, gb, gpart);
 }
 
 }  // namespace
@@ -356,6 +400,36 @@ cudaError_t finish(size_t n, float2 *const ff[4], double *const out[4], cudaStre
   if (!n) return cudaSuccess;
   const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
   ff_finish<<<blocks, 256, 0, s>>>(n, ff[0], ff[1], ff[2], ff[3], out[0], out[1], out[2], out[3]);
+  return cudaGetLastError();
+}
+
+__global__ void ff_accumulate(size_t n, const float2 *a0, const float2 *a1, const float2 *a2,
+                              const float2 *a3, double *o0, double *o1, double *o2, double *o3,
+                              int first) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double v0 = (double)a0[i].x + (double)a0[i].y, v1 = (double)a1[i].x + (double)a1[i].y;
+    const double v2 = (double)a2[i].x + (double)a2[i].y, v3 = (double)a3[i].x + (double)a3[i].y;
+    if (first) {
+      o0[i] = v0;
+      o1[i] = v1;
+      o2[i] = v2;
+      o3[i] = v3;
+    } else {
+      o0[i] += v0;
+      o1[i] += v1;
+      o2[i] += v2;
+      o3[i] += v3;
+    }
+  }
+}
+
+cudaError_t accumulate(size_t n, const float2 *const ff[4], double *const out[4], bool first,
+                       cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+  ff_accumulate<<<blocks, 256, 0, s>>>(n, ff[0], ff[1], ff[2], ff[3], out[0], out[1], out[2],
+                                       out[3], first ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -36,6 +36,12 @@ struct Step {
   float *olv[2] = {nullptr, nullptr};
   float *olt[3] = {nullptr, nullptr, nullptr};
   float2 *g_lm = nullptr, *g_la = nullptr, *g_mu = nullptr, *g_b = nullptr;
+  // Optional FP32 partial sums (lm, la, mu, b) per point of the unpadded
+  // grid: the step's terms are added there, and on a flush step the
+  // partial plus the terms go into the pairs and the partial is reset to 0.
+  // Null: every step adds into the pairs directly.
+  float4 *g_part = nullptr;
+  int flush = 1;
   InjPlan plan{};
   const double *stf = nullptr;
   // Receivers by tile (tiles row-major over ceil(nz / kTZ) columns): tile t
@@ -60,6 +66,9 @@ cudaError_t step(const Maps &maps, const Step &a, cudaStream_t s);
 
 // out[k][i] = hi + lo of the pair ff[k][i] in FP64, k = 0..3, i < n.
 cudaError_t finish(size_t n, float2 *const ff[4], double *const out[4], cudaStream_t s);
+// out[k][i] += hi + lo of ff[k][i] in FP64 (out[k][i] = ... when `first`).
+cudaError_t accumulate(size_t n, const float2 *const ff[4], double *const out[4], bool first,
+                       cudaStream_t s);
 
 }  // namespace exact_tma
 }  // namespace psv

@@ -159,6 +159,7 @@ Model::Model(const Model &o)
 Model::~Model() {
   DeviceGuard guard(device_);
   clear_graphs();
+  destroy_lanes();
   if (stream_) {
     cudaStreamSynchronize(stream_);
     cudaStreamDestroy(stream_);
@@ -551,9 +552,36 @@ cudaError_t Model::tma_adjoint(int shot) {
   return cudaGetLastError();
 }
 
+size_t Model::exact_lane_bytes(int C) const {
+  const int nt = cfg_.nt;
+  if (C <= 0 || C > nt) C = nt;
+  const size_t state = 5 * padded_size() * elem();
+  const size_t n_ck = (nt + C - 1) / C;
+  return n_ck * state + (C + 1) * state + kLamPlanes * padded_size() * elem() +
+         2 * static_cast<size_t>(cfg_.nr) * nt * sizeof(float) + grid_size() * sizeof(float4);
+}
+
+int Model::exact_lane_count(int C, int n_list) const {
+  // As many lanes as shots, at most kMaxLanes, within 60 % of the device
+  // memory that is free or already held by lanes.
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 1;
+  for (const auto &l : lanes_)
+    free_b += l->ckpt.bytes() + l->slots.bytes() + l->lam.bytes() + l->raw.bytes() +
+              l->part.bytes();
+  const size_t per = std::max<size_t>(exact_lane_bytes(C), 1);
+  const size_t fit = static_cast<size_t>(0.6 * static_cast<double>(free_b)) / per;
+  return static_cast<int>(std::max<size_t>(1, std::min<size_t>(
+      fit, static_cast<size_t>(std::min(n_list, kMaxLanes)))));
+}
+
 size_t Model::exact_bytes(int C) const {
   const int nt = cfg_.nt;
   if (C <= 0 || C > nt) C = nt;
+  if (prec_ == PSV_FP32 && tma_ok_ && is_tma())
+    return static_cast<size_t>(exact_lane_count(C, cfg_.n_shots)) * exact_lane_bytes(C) +
+           static_cast<size_t>(cfg_.n_shots) * 4 * grid_size() * sizeof(float2) +
+           7 * grid_size() * sizeof(double);
   const size_t state = 5 * padded_size() * elem();
   const size_t n_ck = (nt + C - 1) / C;
   return n_ck * state + (C + 1) * state + 13 * padded_size() * elem() +
@@ -575,6 +603,7 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
       if (seen[s]++) throw Error(PSV_ERR_INVALID_ARGUMENT, "a shot is listed twice");
     }
   }
+  if (prec_ == PSV_FP32 && tma_ok_ && is_tma()) return exact_gradient_lanes(C, shot_list);
   const int nt = cfg_.nt, n_shots = cfg_.n_shots, nr = cfg_.nr;
   if (C <= 0 || C > nt) C = nt;
   const int n_ck = (nt + C - 1) / C;
@@ -874,6 +903,311 @@ double Model::exact_gradient(int C, const std::vector<int> &shot_list) {
              "exact chain");
   synchronize();
   if (tma || etma) check_device_error();
+  return misfit;
+}
+
+void Model::destroy_lanes() {
+  for (auto &l : lanes_) {
+    if (l->stream) {
+      cudaStreamSynchronize(l->stream);
+      cudaStreamDestroy(l->stream);
+    }
+    if (l->done) cudaEventDestroy(l->done);
+  }
+  lanes_.clear();
+  if (lanes_start_) {
+    cudaEventDestroy(lanes_start_);
+    lanes_start_ = nullptr;
+  }
+}
+
+// FP32 exact gradient with the TMA steps, the shots in concurrent lanes.
+// Per shot, in its lane (stream order), the same pipeline as the serial
+// path: a checkpoint pass (the forward run slot to slot, its state saved
+// every C steps, its receivers recorded), the seismograms and adjoint
+// receiver terms, then the segments backwards, each recomputed from its
+// checkpoint into the C + 1 state slots and transposed step by step into
+// the shot's own gradient sums. Every forward step, in either pass, is the
+// same TMA step kernel from slot j into slot j + 1, so every state is the
+// same whatever C. Each shot's pipeline is captured once as a CUDA graph on
+// its lane's stream and replayed. At the end the shots' sums are added in
+// shot order, and the chain rule maps them to (vp, vs, rho).
+double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
+  const int nt = cfg_.nt, n_shots = cfg_.n_shots, nr = cfg_.nr;
+  if (C <= 0 || C > nt) C = nt;
+  const int n_ck = (nt + C - 1) / C;
+  const size_t gp = padded_size(), g = grid_size();
+  const size_t field_bytes = gp * sizeof(float), state_bytes = 5 * field_bytes;
+  cudaStream_t ms = stream();
+  const int n_list = static_cast<int>(shot_list.size());
+  const int K = std::max(1, exact_lane_count(C, std::max(n_list, 1)));
+
+  bool grown = false;
+  auto ensure = [&](DeviceBuffer &b, size_t bytes) {
+    if (b.bytes() < bytes) {
+      synchronize();
+      for (auto &l : lanes_)
+        if (l->stream) cuda_check(cudaStreamSynchronize(l->stream), "lane sync");
+      b.allocate(bytes);
+      grown = true;
+    }
+  };
+  // Lanes beyond K give their memory back.
+  while (static_cast<int>(lanes_.size()) > K) {
+    auto &l = lanes_.back();
+    if (l->stream) {
+      cuda_check(cudaStreamSynchronize(l->stream), "lane sync");
+      cudaStreamDestroy(l->stream);
+    }
+    if (l->done) cudaEventDestroy(l->done);
+    lanes_.pop_back();
+    grown = true;
+  }
+  while (static_cast<int>(lanes_.size()) < K) {
+    auto l = std::make_unique<ExactLane>();
+    if (!lanes_.empty())
+      cuda_check(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking), "lane stream");
+    cuda_check(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming), "lane event");
+    lanes_.push_back(std::move(l));
+    grown = true;
+  }
+  if (!lanes_start_)
+    cuda_check(cudaEventCreateWithFlags(&lanes_start_, cudaEventDisableTiming), "lane event");
+  for (auto &l : lanes_) {
+    ensure(l->ckpt, n_ck * state_bytes);
+    ensure(l->slots, (C + 1) * state_bytes);
+    ensure(l->lam, kLamPlanes * field_bytes);
+    ensure(l->raw, std::max<size_t>(2 * static_cast<size_t>(nr) * nt * sizeof(float), 16));
+    ensure(l->part, g * sizeof(float4));
+  }
+  for (auto &b : gex_) ensure(b, g * sizeof(double));
+  for (auto &b : kexact_) ensure(b, g * sizeof(double));
+  for (auto &b : adj_) ensure(b, data_size() * sizeof(double));
+  ensure(gff_shots_, static_cast<size_t>(n_shots) * 4 * g * sizeof(float2));
+  if (grown) clear_graphs();
+
+  // Tensor maps of each lane's slots (forward steps) and of its adjoint
+  // planes, slots and the medium (exact steps); encoded when the buffers,
+  // C or the tile shape change.
+  auto slot_fields = [&](ExactLane &l, int j) {
+    float *b = reinterpret_cast<float *>(l.slots.as<unsigned char>() + j * state_bytes);
+    const size_t n = gp;
+    return fast::Fields{b, b + n, b + 2 * n, b + 3 * n, b + 4 * n};
+  };
+  for (auto &lp : lanes_) {
+    ExactLane &l = *lp;
+    if (l.maps_slots == l.slots.get() && l.maps_lam == l.lam.get() && l.maps_C == C &&
+        l.maps_cfg == tile_cfg_)
+      continue;
+    l.slot_maps.assign(C + 1, tma::Maps{});
+    for (int j = 0; j <= C; ++j)
+      if (!tma::encode_input_maps(l.slot_maps[j], slot_fields(l, j), lm_.as<float>(),
+                                  mu_.as<float>(), geo_.nx, geo_.nz, pitch_, tile_cfg_))
+        throw Error(PSV_ERR_CUDA, "tensor-map encoding failed for a state slot");
+    if (!exact_tma::encode(l.emaps, l.lam.as<float>(), kLamPlanes, l.slots.as<float>(),
+                           5 * (C + 1), field_bytes, lm_.as<float>(), la_.as<float>(),
+                           mu_.as<float>(), b_.as<float>(), geo_.nx, geo_.nz, pitch_))
+      throw Error(PSV_ERR_CUDA, "tensor-map encoding failed for the exact adjoint");
+    l.maps_slots = l.slots.get();
+    l.maps_lam = l.lam.get();
+    l.maps_C = C;
+    l.maps_cfg = tile_cfg_;
+  }
+
+  auto one_shot = [&](ExactLane &l, int shot, cudaStream_t s) {
+    unsigned char *ck = l.ckpt.as<unsigned char>(), *sl = l.slots.as<unsigned char>();
+    float2 *gs = gff_shots_.as<float2>() + static_cast<size_t>(shot) * 4 * g;
+    cuda_check(cudaMemsetAsync(gs, 0, 4 * g * sizeof(float2), s), "exact zero");
+    cuda_check(cudaMemsetAsync(l.part.get(), 0, g * sizeof(float4), s), "exact zero");
+    auto state = [&](unsigned char *base, void *out[5]) {
+      for (int f = 0; f < 5; ++f) out[f] = base + f * field_bytes;
+    };
+    auto copy = [&](unsigned char *from, unsigned char *to) {
+      void *src[5], *dst[5];
+      state(from, src);
+      state(to, dst);
+      cuda_check(copy_state(src, dst, nullptr, field_bytes, s), "copy state");
+    };
+    float *raw = l.raw.as<float>();
+    // Steps it0 .. it1-1 from slot 0 (state it0) into slots 1 .. it1-it0.
+    auto slots_forward = [&](int it0, int it1, bool record) {
+      for (int n = it0; n < it1; ++n) {
+        const int j = n - it0;
+        tma::SimDesc d = descs_h_[shot];
+        d.set[0] = slot_fields(l, j);
+        d.set[1] = slot_fields(l, j + 1);
+        d.maps[0] = l.slot_maps[j];
+        d.rec_vx = raw;
+        d.rec_vz = raw + static_cast<size_t>(nr) * nt;
+        if (!record) d.nr = 0;
+        cuda_check(tma::step_single(d, tile_cfg_, false, n, 0, false, err_flag_.as<int>(), s),
+                   "exact forward");
+      }
+    };
+    // Checkpoint pass.
+    cuda_check(cudaMemsetAsync(sl, 0, state_bytes, s), "zero state");
+    for (int k = 0; k < n_ck; ++k) {
+      const int s0 = k * C, s1 = std::min(nt, s0 + C);
+      copy(sl, ck + k * state_bytes);
+      slots_forward(s0, s1, true);
+      if (k + 1 < n_ck) copy(sl + (s1 - s0) * state_bytes, sl);
+    }
+    const size_t off = static_cast<size_t>(shot) * nr * nt;
+    if (nr) {
+      cuda_check(receiver_cumsum_f32(nr, nt, nt, cfg_.dt, cfg_.dx * cfg_.dz, raw,
+                                     raw + static_cast<size_t>(nr) * nt,
+                                     rtf_[0].as<double>() + off, rtf_[1].as<double>() + off, s),
+                 "seismograms");
+      for (int c = 0; c < 2; ++c)
+        cuda_check(exact_receiver_terms(nr, nt, cfg_.dt, cfg_.dx * cfg_.dz,
+                                        rtf_[c].as<double>() + off,
+                                        rtf_true_[c].as<double>() + off,
+                                        adj_[c].as<double>() + off, s),
+                   "receiver terms");
+    }
+    cuda_check(cudaMemsetAsync(l.lam.get(), 0, l.lam.bytes(), s), "zero adjoint");
+    // Adjoint state planes: l^{n+1} in (lv, lt), l^n out (ov, ot), swapped
+    // after every step.
+    int lv[2] = {0, 1}, ov[2] = {8, 9}, lt[3] = {2, 3, 4}, ot[3] = {5, 6, 7};
+    auto plane = [&](int k) { return l.lam.as<unsigned char>() + k * field_bytes; };
+    for (int k = n_ck - 1; k >= 0; --k) {
+      const int s0 = k * C, s1 = std::min(nt, s0 + C);
+      if (k + 1 < n_ck) {  // the last segment's states are still in the slots
+        copy(ck + k * state_bytes, sl);
+        slots_forward(s0, s1, false);
+      }
+      for (int n = s1 - 1; n >= s0; --n) {
+        exact_tma::Step x;
+        x.nx = geo_.nx;
+        x.nz = geo_.nz;
+        x.pitch = pitch_;
+        x.np = cfg_.np_boundary;
+        x.nt = nt;
+        x.it = n;
+        x.dt = static_cast<float>(cfg_.dt);
+        x.idx = static_cast<float>(1.0 / cfg_.dx);
+        x.idz = static_cast<float>(1.0 / cfg_.dz);
+        x.dt_d = cfg_.dt;
+        x.taper_tab = taper_tab_d_.as<float>();
+        for (int f = 0; f < 2; ++f) {
+          x.lv[f] = lv[f];
+          x.olv[f] = reinterpret_cast<float *>(plane(ov[f]));
+        }
+        for (int f = 0; f < 3; ++f) {
+          x.lt[f] = lt[f];
+          x.olt[f] = reinterpret_cast<float *>(plane(ot[f]));
+        }
+        x.sv = 5 * (n - s0);
+        x.st = 5 * (n + 1 - s0);
+        x.g_lm = gs;
+        x.g_la = gs + g;
+        x.g_mu = gs + 2 * g;
+        x.g_b = gs + 3 * g;
+        // Terms go into FP32 partial sums, added into the float-float pairs
+        // every kFlushSteps steps and at step 0.
+        x.g_part = l.part.as<float4>();
+        x.flush = (n % kFlushSteps == 0) ? 1 : 0;
+        x.plan = plans_[shot];
+        x.stf = stf_d_.as<double>();
+        x.rec_cell = rec_cell_.as<int>();
+        x.rec_start = exrec_start_.as<int>();
+        x.rec_list = exrec_list_.as<int>();
+        x.adj_x = adj_[0].as<double>() + off;
+        x.adj_z = adj_[1].as<double>() + off;
+        x.err = err_flag_.as<int>();
+        cuda_check(exact_tma::step(l.emaps, x, s), "exact step");
+        for (int f = 0; f < 2; ++f) std::swap(lv[f], ov[f]);
+        for (int f = 0; f < 3; ++f) std::swap(lt[f], ot[f]);
+      }
+    }
+  };
+
+  // Lanes start after the work already queued on the model's stream.
+  cuda_check(cudaEventRecord(lanes_start_, ms), "lane start");
+  for (int k = 1; k < K; ++k)
+    cuda_check(cudaStreamWaitEvent(lanes_[k]->stream, lanes_start_, 0), "lane wait");
+  for (int i = 0; i < n_list; ++i) {
+    const int shot = shot_list[i];
+    const int li = i % K;
+    ExactLane &l = *lanes_[li];
+    cudaStream_t s = li == 0 ? ms : l.stream;
+    auto enqueue = [&] { one_shot(l, shot, s); };
+    if (!use_graphs_) {
+      enqueue();
+      continue;
+    }
+    GraphEntry &ge = graphs_[std::make_tuple(3 + li, shot, K, C)];
+    if (ge.exec) {
+      cuda_check(cudaGraphLaunch(ge.exec, s), "cudaGraphLaunch");
+      continue;
+    }
+    if (ge.uses++ == 0) {  // first run: eager
+      enqueue();
+      continue;
+    }
+    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+               "cudaStreamBeginCapture");
+    try {
+      enqueue();
+    } catch (...) {
+      cudaGraph_t broken = nullptr;
+      cudaStreamEndCapture(s, &broken);
+      if (broken) cudaGraphDestroy(broken);
+      throw;
+    }
+    cudaGraph_t graph = nullptr;
+    cuda_check(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
+    cudaError_t e = cudaGraphInstantiate(&ge.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    cuda_check(e, "cudaGraphInstantiate");
+    cuda_check(cudaGraphLaunch(ge.exec, s), "cudaGraphLaunch");
+  }
+  for (int k = 1; k < K; ++k) {
+    cuda_check(cudaEventRecord(lanes_[k]->done, lanes_[k]->stream), "lane done");
+    cuda_check(cudaStreamWaitEvent(ms, lanes_[k]->done, 0), "lane join");
+  }
+
+  double misfit = 0;
+  if (n_list == n_shots) {
+    misfit = calculate_l2_misfit();
+  } else {
+    const size_t per = static_cast<size_t>(nr) * nt;
+    for (int shot : shot_list) {
+      if (!per) break;
+      const size_t off = static_cast<size_t>(shot) * per;
+      int parts = static_cast<int>(std::min<size_t>(kPartials, (per + 255) / 256));
+      if (parts < 1) parts = 1;
+      cuda_check(misfit_l2(per, cfg_.dt, rtf_true_[0].as<double>() + off, rtf_[0].as<double>() + off,
+                           rtf_true_[1].as<double>() + off, rtf_[1].as<double>() + off,
+                           partials_.as<double>(), parts, scalar_.as<double>(), ms),
+                 "shot misfit");
+      double v = 0;
+      cuda_check(cudaMemcpyAsync(&v, scalar_.get(), sizeof(double), cudaMemcpyDeviceToHost, ms),
+                 "misfit copy");
+      synchronize();
+      misfit += v;
+    }
+    misfit_ = misfit;
+  }
+  // The shots' sums in increasing shot order (independent of the lanes).
+  std::vector<int> order(shot_list);
+  std::sort(order.begin(), order.end());
+  double *out[4] = {gex_[0].as<double>(), gex_[1].as<double>(), gex_[2].as<double>(),
+                    gex_[3].as<double>()};
+  if (order.empty())
+    for (auto &b : gex_) cuda_check(cudaMemsetAsync(b.get(), 0, b.bytes(), ms), "exact zero");
+  for (size_t i = 0; i < order.size(); ++i) {
+    const float2 *gs = gff_shots_.as<float2>() + static_cast<size_t>(order[i]) * 4 * g;
+    const float2 *ff[4] = {gs, gs + g, gs + 2 * g, gs + 3 * g};
+    cuda_check(exact_tma::accumulate(g, ff, out, i == 0, ms), "exact sums");
+  }
+  cuda_check(exact_chain(g, vp_.as<double>(), vs_.as<double>(), rho_.as<double>(),
+                         gex_[0].as<double>(), gex_[1].as<double>(), gex_[2].as<double>(),
+                         gex_[3].as<double>(), kexact_[0].as<double>(), kexact_[1].as<double>(),
+                         kexact_[2].as<double>(), ms),
+             "exact chain");
+  synchronize();
+  check_device_error();
   return misfit;
 }
 

@@ -14,6 +14,7 @@
 
 #include "psv_config.hpp"
 #include "psv_solver.hpp"
+#include "psv_exact_tma.hpp"
 #include "psv_tma.hpp"
 
 namespace psv {
@@ -274,6 +275,31 @@ class Model {
   DeviceBuffer gex_[4], kexact_[3], adj_[2], lam_, ckpt_, slots_;
   DeviceBuffer exrec_start_, exrec_list_;  // receivers by tile of the exact TMA step
   DeviceBuffer gff_[4];  // FP32 exact step: float-float gradient sums (lm, la, mu, b)
+  // FP32 exact adjoint with the TMA steps: the shots of a gradient run
+  // concurrently in lanes, each lane a stream (lane 0: the model's) with its
+  // own checkpoints, state slots, adjoint planes and raw receiver series;
+  // shot k of a gradient runs in lane k % lanes. The gradient sums are kept
+  // per shot ([n_shots][4][grid] float-float pairs) and added up in shot
+  // order at the end, so the result does not depend on the lane count.
+  struct ExactLane {
+    cudaStream_t stream = nullptr;  // own stream (lanes >= 1)
+    cudaEvent_t done = nullptr;
+    DeviceBuffer ckpt, slots, lam, raw, part;  // part: FP32 partial gradient sums
+    std::vector<tma::Maps> slot_maps;  // input maps of each state slot
+    exact_tma::Maps emaps;             // the exact step's maps over lam, slots, medium
+    const void *maps_slots = nullptr;  // slots / lam / C / tile shape the maps were made for
+    const void *maps_lam = nullptr;
+    int maps_C = -1, maps_cfg = -1;
+  };
+  std::vector<std::unique_ptr<ExactLane>> lanes_;
+  DeviceBuffer gff_shots_;
+  cudaEvent_t lanes_start_ = nullptr;
+  static constexpr int kMaxLanes = 8;
+  static constexpr int kFlushSteps = 10;  // exact step: partial sums into the pairs
+  int exact_lane_count(int C, int n_list) const;
+  size_t exact_lane_bytes(int C) const;
+  double exact_gradient_lanes(int C, const std::vector<int> &shot_list);
+  void destroy_lanes();
   // Injection plans: one per shot (sources) and one for the adjoint receivers.
   std::vector<DeviceBuffer> plan_terms_, plan_maps_;
   std::vector<InjPlan> plans_;  // [n_shots] forward, [n_shots] = adjoint
