@@ -262,6 +262,19 @@ def fwi_gradients_c3(steps, with_cpu=False):
             res["device_bytes"] = m.exact_bytes(kw["checkpoint_every"])
         out[name] = res
     out["value"] = out["checkpoint_100"]["value"]
+    # Algorithmic bytes of one checkpointed gradient: per shot and step two
+    # forward steps (checkpoint pass, recompute; 52 B per cell each) and one
+    # exact step (114.4 B per cell: 19 words of fields and medium, FP32
+    # partial sums read and written, float-float pairs on one step in ten).
+    cells = float(m.nx * m.nz)
+    per_grad = m.n_shots * m.nt * cells * (2 * 52.0 + 114.4)
+    peak, kind = measured_peaks()
+    t = out["checkpoint_100"]["ms_per_gradient"] / 1e3
+    out["roofline"] = {"bound": "hbm", "bytes_per_gradient": per_grad,
+                       "achieved": per_grad / t / 1e9, "peak": peak, "unit": "GB/s",
+                       "frac": per_grad / t / 1e9 / peak, "peak_source": kind,
+                       "note": "whole checkpointed gradient, all kernels, 8 shots in "
+                               "concurrent lanes"}
     if with_cpu:
         out["cpu_baseline"] = cpu_baseline_c3()
     return out
@@ -296,18 +309,22 @@ def cpu_baseline_c3(n_steps=600):
 
 
 def mc_samples_c4():
-    """Accepted MC samples/s on the surrogate workload (c0 grid, 600 coarse
-    parameters): delayed-acceptance HMC screened by the trained network
-    (4096 prior triples + 512 local triples here; python -m
-    psvwave_gb300.c4 runs the full 20000), against HMC with the solver's
-    exact gradients and against screening by the prior alone."""
+    """Accepted MC samples/s on the surrogate workload at its stated size (c0
+    grid, 600 coarse parameters): the network trained on 20000 exact
+    (model, misfit, gradient) triples plus 1024 local ones, then
+    delayed-acceptance HMC over 128 chains x 400 iterations (51200
+    proposals) screened by the network, against the same sampler screened
+    by the prior alone and against HMC with the solver's exact gradients
+    (16 chains x 32 iterations, 512 samples), with posterior summaries of
+    the exact samplers (psvwave_gb300.c4)."""
     from psvwave_gb300 import c4
 
-    out = c4.run(n_train=4096, n_local=512, n_chains=128, n_iter=40, plain_iter=3)
+    out = c4.run(n_train=20000, n_local=1024, n_chains=128, n_iter=400, plain_chains=16,
+                 plain_iter=32)
     out["unit"] = "accepted samples/s"
     out["workload"] = ("c4: 250x150 grid, nt=2000, Ricker 15 Hz, 600 coarse parameters "
                        "(20x10 vp/vs/rho, prior sigma 10%), s2 = misfit(prior mean)/20; "
-                       "128 chains")
+                       "20000 training triples, 128 chains x 400 iterations")
     return out
 
 
@@ -612,9 +629,15 @@ def main():
     kernel_avg_ms = max_ms / args.steps / nt
     achieved = bpc * cells / (kernel_avg_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
+    traffic = measured_traffic(dominant)
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": measured_traffic(dominant), "bytes_per_launch": bpc * cells,
+                "traffic": traffic,
+                # measured DRAM bytes per step (warm-cache ncu capture) over
+                # this run's time per step, against the same peak
+                "dram_frac": (traffic / (kernel_avg_ms / 1e3) / 1e9 / peak
+                              if traffic else None),
+                "bytes_per_launch": bpc * cells,
                 "kernel_avg_ms_timed_region": kernel_avg_ms,
                 "launch_scheme": model.kernel_variant,
                 "isolated_kernel_ms": kernel_ms, "isolated_step_ms": per_step_ms,
