@@ -91,6 +91,12 @@ decltype(auto) with_shape(int cfg, F &&f) {
   return f(ShapeTag<Big, kTile32x60>{});
 }
 
+// A call made between phase B and phase C of a tile (the persistent step
+// draws its next item there).
+struct NoHook {
+  __device__ void operator()() const {}
+};
+
 // An interior tile computes every stress point of its box (rows X0-2 ..
 // X0+TX+1, columns Z0-2 .. Z0+TZ+1) inside the updated region 2 <= x < n-2
 // and at least np frames deep (taper exactly 1), has no source or
@@ -137,13 +143,13 @@ __device__ __forceinline__ float col_taper(const SimDesc &d, int gz) {
 // rows of one column, keeping the x-direction stencil values of vx and vz in
 // registers (one new shared load each per row); phase C: KC consecutive
 // rows per thread with the x-direction windows of txx and txz.
-template <class S, bool ADJ, bool TAPER>
+template <class S, bool ADJ, bool TAPER, class Mid = NoHook>
 __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields &out, int X0,
                                             int Z0, const float (*VX)[S::W],
                                             const float (*VZ)[S::W], float (*sxx_)[S::W],
                                             float (*szz_)[S::W], float (*sxz_)[S::W],
                                             const float (*slm)[S::W], const float (*smu)[S::W],
-                                            const float *bb) {
+                                            const float *bb, const Mid &mid = Mid()) {
   constexpr int TX = S::TX, TZ = S::TZ, SR = S::SR, G = S::G;
   constexpr int KC = TX / G;
   const int ps = d.pitch;
@@ -206,6 +212,7 @@ __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields
     }
   }
   __syncthreads();
+  mid();
   if (lzc < TZ) {
     const float(*TXX)[S::W] = sxx_;
     const float(*TZZ)[S::W] = szz_;
@@ -295,13 +302,13 @@ __device__ __forceinline__ void sts2(float *p, float2 v) { *reinterpret_cast<flo
 // rows beyond the grid's last row are skipped).
 // bb: this thread's buoyancy, rows X0 + KV w + k (KV = TX / warps own rows
 // per warp), columns Z0 + 2 lane + {0,1}.
-template <class S, bool ADJ, bool FRAME>
+template <class S, bool ADJ, bool FRAME, class Mid = NoHook>
 __device__ __forceinline__ void tile_phases_v2(const SimDesc &d, const fast::Fields &out, int X0,
                                                int Z0, const float (*VX)[S::W],
                                                const float (*VZ)[S::W], float (*sxx_)[S::W],
                                                float (*szz_)[S::W], float (*sxz_)[S::W],
                                                const float (*slm)[S::W], const float (*smu)[S::W],
-                                               const float *bb) {
+                                               const float *bb, const Mid &mid = Mid()) {
   static_assert(S::TZ == 60, "two columns per lane over the 64 stress columns");
   constexpr int TX = S::TX, TZ = S::TZ, WARPS = S::WARPS, SR = S::SR;
   // Stress rows: warp w takes RQ or RQ + 1 consecutive rows; own rows: KV.
@@ -394,6 +401,7 @@ __device__ __forceinline__ void tile_phases_v2(const SimDesc &d, const fast::Fie
     }
   }
   __syncthreads();
+  mid();
   if (lane < TZ / 2) {
     const float(*TXX)[S::W] = sxx_;
     const float(*TZZ)[S::W] = szz_;
@@ -475,11 +483,11 @@ __device__ __forceinline__ void tile_phases_v2(const SimDesc &d, const fast::Fie
 // 32 x 60, whose 2100 x 900 persistent step it slowed by 1.5 %. A shape
 // uses the same paths in every kernel, so per-step and persistent launches
 // give the same bits.
-template <class S, int CFG, bool ADJ, bool TAPERED = (S::NT == 128)>
+template <class S, int CFG, bool ADJ, bool TAPERED = (S::NT == 128), class Mid = NoHook>
 __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, int X0, int Z0,
                                           bool first, int tile, int it, int parity, int store,
                                           int *err, uint32_t phase, bool init_bar,
-                                          bool sync_copy = true) {
+                                          bool sync_copy = true, const Mid &mid = Mid()) {
   constexpr int TX = S::TX, TZ = S::TZ, W = S::W, VR = S::VR, SR = S::SR, G = S::G;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>(
@@ -610,21 +618,21 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
 
   if constexpr (V2) {
     if (inner) {
-      tile_phases_v2<S, ADJ, false>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
+      tile_phases_v2<S, ADJ, false>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb, mid);
       return true;
     }
     if (frame) {
-      tile_phases_v2<S, ADJ, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
+      tile_phases_v2<S, ADJ, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb, mid);
       return true;
     }
   } else {
     if (inner) {
-      tile_phases<S, ADJ, false>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
+      tile_phases<S, ADJ, false>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb, mid);
       return true;
     }
   }
   if (TAPERED && tapered) {
-    tile_phases<S, ADJ, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb);
+    tile_phases<S, ADJ, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb, mid);
     return true;
   }
 
@@ -689,6 +697,7 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
     }
   }
   __syncthreads();
+  mid();
 
   // Phase C: new velocities of the tile's own points.
   if (col_ok) {
@@ -767,18 +776,26 @@ __device__ __forceinline__ bool wait_at_least(const unsigned *p, unsigned v) {
 }
 
 // All time steps of one simulation in one launch. sched[0] hands out items
-// w = step * n_tiles + tile in increasing order (a CTA holds at most its
-// current item and the next); sched[1 + t] counts the steps tile t has
-// finished. An item starts once the tile and its eight
+// w = step * n_tiles + tile in increasing order; sched[1 + t] counts the
+// steps tile t has finished. An item starts once the tile and its eight
 // neighbours have finished the previous step: that is everything the step
 // reads (halos are at most 4 points, less than a tile), and it also
 // guarantees that no neighbour still reads the buffer the step overwrites.
 // The earliest unfinished item always has its inputs ready, so the
 // schedule cannot deadlock; each wait is bounded nonetheless, and a CTA
 // that gives up raises *err and stops (its dependents then time out too).
-// Publication is a barrier followed by one thread's st.release.gpu: release
-// is cumulative, so it orders every store of the CTA that precedes the
-// barrier, and the waiting side's ld.acquire.gpu sees them all.
+//
+// Thread 0 draws the CTA's next item between phases B and C of the current
+// one: the atomic's latency hides behind phase C, and a CTA holds a second
+// item only for that last part of an item. Drawn earlier, the CTAs held
+// about one step's worth of items between them (456 CTAs, 990 tiles), so
+// an item often reached its neighbours' previous step before they had
+// finished it.
+// Publication: after the item's closing barrier the last thread of the CTA
+// (idle in phase C) issues one st.release.gpu. Release is cumulative, so it
+// orders every store of the CTA that precedes the barrier, and the waiting
+// side's ld.acquire.gpu sees them all; its wait for the item's stores to
+// drain overlaps the next item's polls and copies.
 template <class S, int CFG, bool ADJ>
 __global__ void __launch_bounds__(S::NT, S::MINB)
     fused_steps_tma(const __grid_constant__ SimDesc d, int tiles_x, int tiles_z, int it0,
@@ -786,32 +803,15 @@ __global__ void __launch_bounds__(S::NT, S::MINB)
   __shared__ int s_item;
   const int n_tiles = tiles_x * tiles_z;
   const long long total = (long long)n_steps * n_tiles;
+  constexpr int PUB = S::NT - 1;
   uint32_t phase = 0;
   bool init = true;
-  // Thread 0 holds the item after the current one and the finished item it
-  // has yet to publish. Per item, after the barrier that ends the previous
-  // one: thread 0 publishes that item (fence + release) while warp 1's first
-  // nine lanes poll the new item's neighbours, and one barrier lets the CTA
-  // go on. A poll may wait on this CTA's own publication, which thread 0
-  // makes without waiting on anything.
   unsigned next = 0;
-  int pub_tile = -1;
-  unsigned pub_count = 0;
-  if (threadIdx.x == 0) {
-    s_item = (int)atomicAdd(sched, 1u);
-    next = atomicAdd(sched, 1u);
-  }
+  if (threadIdx.x == 0) s_item = (int)atomicAdd(sched, 1u);
   __syncthreads();
   for (;;) {
     const long long w = s_item;
-    if (w >= total) {
-      if (threadIdx.x == 0 && pub_tile >= 0) {
-        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + pub_tile),
-                     "r"(pub_count)
-                     : "memory");
-      }
-      return;
-    }
+    if (w >= total) return;
     const int j = (int)(w / n_tiles), tile = (int)(w - (long long)j * n_tiles);
     const int tx = tile / tiles_z, tz = tile - tx * tiles_z;
     bool ok = true;
@@ -821,35 +821,28 @@ __global__ void __launch_bounds__(S::NT, S::MINB)
       if (a >= 0 && a < tiles_x && b >= 0 && b < tiles_z)
         ok = wait_at_least(sched + 1 + a * tiles_z + b, (unsigned)j);
     }
-    if (threadIdx.x == 0 && pub_tile >= 0) {
-      // The release orders everything that precedes it in causality order:
-      // every thread's stores of the item, through the barrier that ended it.
-      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + pub_tile),
-                   "r"(pub_count)
-                   : "memory");
-      pub_tile = -1;
-    }
     if (!__syncthreads_and(ok)) {
       if (threadIdx.x == 0) atomicOr(err, 2);
       return;
     }
-    // The copies (async proxy) must see what the generic stores of other
-    // CTAs made visible to the polling threads.
     if (j > 0 && threadIdx.x == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
     const int it = ADJ ? it0 - j : it0 + j;
     const int parity = parity0 ^ (j & 1);
-    if (!step_body<S, CFG, ADJ>(d, d.maps[parity], tx * S::TX, tz * S::TZ, false, tile, it,
-                                parity, store, err, phase, init, init))
+    const auto draw = [&]() {
+      if (threadIdx.x == 0) next = atomicAdd(sched, 1u);
+    };
+    if (!step_body<S, CFG, ADJ, (S::NT == 128)>(d, d.maps[parity], tx * S::TX, tz * S::TZ, false,
+                                                 tile, it, parity, store, err, phase, init,
+                                                 init, draw))
       return;
     phase ^= 1u;
     init = false;
-    if (threadIdx.x == 0) {
-      pub_tile = tile;
-      pub_count = (unsigned)(j + 1);
-      s_item = (int)next;
-      next = atomicAdd(sched, 1u);
-    }
-    __syncthreads();  // every thread's stores of the item are issued; s_item is the next item
+    if (threadIdx.x == 0) s_item = (int)next;
+    __syncthreads();
+    if (threadIdx.x == PUB)
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(sched + 1 + tile),
+                   "r"((unsigned)(j + 1))
+                   : "memory");
   }
 }
 
