@@ -6,7 +6,8 @@
 // terms to the gradients of lm, la, mu and b. Each CTA owns a
 // kTX x kTZ tile. Thread 0 issues fourteen tiled bulk-tensor copies that
 // complete on one mbarrier: b, lv with a 4-point halo in both axes; lt, lm,
-// la, mu, v^n and tau^{n+1} with a 2-point halo (all boxes kTZ + 8 wide,
+// mu, v^n and tau^{n+1} with a 2-point halo (lambda = lm - 2 mu, formed in
+// registers as the forward TMA step forms it) (all boxes kTZ + 8 wide,
 // starting 4 columns left of the tile so that they stay 16-byte aligned;
 // the copies zero-fill outside the grid). The medium is issued before the
 // programmatic-dependent-launch wait (it does not change during a gradient),
@@ -74,7 +75,10 @@ constexpr int OFF_FT = OFF_FV + 2 * SB;     // txx, tzz, txz of tau^{n+1}
 constexpr int OFF_W = OFF_FT + 3 * SB;      // wx, wz
 constexpr int OFF_P = OFF_M;                // px, pz, q over lm, la, mu (same points)
 constexpr int TOTAL = OFF_W + 2 * VB;
-constexpr int TX_BYTES = OFF_W * 4;         // delivered by the copies
+// Delivered by the copies: every box but la's (lambda is lm - 2 mu, formed
+// in registers as the forward TMA step forms it; its box is left empty and
+// later holds p_z).
+constexpr int TX_BYTES = (OFF_W - SB) * 4;
 constexpr int SMEM = TOTAL * 4 + 16 + 128;  // + mbarrier + alignment slack
 constexpr int ROWS = TX / (NT / 32);        // own rows per thread
 static_assert((VB * 4) % 128 == 0 && (SB * 4) % 128 == 0, "boxes must stay 128-byte aligned");
@@ -131,7 +135,7 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
   __syncthreads();
 
   float *LXX = sm + OFF_LT, *LZZ = sm + OFF_LT + SB, *LXZ = sm + OFF_LT + 2 * SB;
-  const float *LM = sm + OFF_M, *LA = sm + OFF_M + SB, *MU = sm + OFF_M + 2 * SB;
+  const float *LM = sm + OFF_M, *MU = sm + OFF_M + 2 * SB;
   float *PX = sm + OFF_P, *PZ = sm + OFF_P + SB, *QQ = sm + OFF_P + 2 * SB;
   // Phase 2: lt~ = lt - (A^T w terms), and p_x = dt (lm y_xx + la y_zz),
   // p_z = dt (la y_xx + lm y_zz), q = dt mu y_xz with y = T lt~ on I, 0
@@ -154,7 +158,8 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
       LZZ[s] = lzz;
       LXZ[s] = lxz;
       if (INNER) {
-        const float lm = LM[s], la = LA[s], mu = MU[s];
+        const float lm = LM[s], mu = MU[s];
+        const float la = lm - 2.0f * mu;
         px = a.dt * (lm * lxx + la * lzz);
         pz = a.dt * (la * lxx + lm * lzz);
         q = a.dt * mu * lxz;
@@ -162,7 +167,8 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
         const float tp = taper_at(a, ix, jz);
         const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
         if (!(yxx == 0.f && yzz == 0.f && yxz == 0.f)) {
-          const float lm = LM[s], la = LA[s], mu = MU[s];
+          const float lm = LM[s], mu = MU[s];
+          const float la = lm - 2.0f * mu;
           px = a.dt * (lm * yxx + la * yzz);
           pz = a.dt * (la * yxx + lm * yzz);
           q = a.dt * mu * yxz;
@@ -303,7 +309,6 @@ __global__ void __launch_bounds__(NT, 4)
                  : "memory");
     tma_load_2d(sm + OFF_B, &maps.b, Z0 - 4, X0 - 4, bar);
     tma_load_2d(sm + OFF_M, &maps.lm, Z0 - 4, X0 - 2, bar);
-    tma_load_2d(sm + OFF_M + SB, &maps.la, Z0 - 4, X0 - 2, bar);
     tma_load_2d(sm + OFF_M + 2 * SB, &maps.mu, Z0 - 4, X0 - 2, bar);
   }
   __syncthreads();  // the initialised mbarrier, before anyone waits on it

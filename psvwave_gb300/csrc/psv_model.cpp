@@ -1041,28 +1041,40 @@ double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
       cuda_check(copy_state(src, dst, nullptr, field_bytes, s), "copy state");
     };
     float *raw = l.raw.as<float>();
+    // Step n from slot j_in into slot j_out.
+    auto step = [&](int n, int j_in, int j_out, bool record) {
+      tma::SimDesc d = descs_h_[shot];
+      d.set[0] = slot_fields(l, j_in);
+      d.set[1] = slot_fields(l, j_out);
+      d.maps[0] = l.slot_maps[j_in];
+      d.rec_vx = raw;
+      d.rec_vz = raw + static_cast<size_t>(nr) * nt;
+      if (!record) d.nr = 0;
+      cuda_check(tma::step_single(d, ecfg, false, n, 0, false, err_flag_.as<int>(), s),
+                 "exact forward");
+    };
     // Steps it0 .. it1-1 from slot 0 (state it0) into slots 1 .. it1-it0.
     auto slots_forward = [&](int it0, int it1, bool record) {
-      for (int n = it0; n < it1; ++n) {
-        const int j = n - it0;
-        tma::SimDesc d = descs_h_[shot];
-        d.set[0] = slot_fields(l, j);
-        d.set[1] = slot_fields(l, j + 1);
-        d.maps[0] = l.slot_maps[j];
-        d.rec_vx = raw;
-        d.rec_vz = raw + static_cast<size_t>(nr) * nt;
-        if (!record) d.nr = 0;
-        cuda_check(tma::step_single(d, ecfg, false, n, 0, false, err_flag_.as<int>(), s),
-                   "exact forward");
-      }
+      for (int n = it0; n < it1; ++n) step(n, n - it0, n - it0 + 1, record);
     };
-    // Checkpoint pass.
+    // Checkpoint pass. Every segment but the last runs back and forth
+    // between slots 0 and 1 (two states that stay in L2, where C + 1 slots
+    // would stream through DRAM); the last one runs into slots 1 .. for the
+    // reverse sweep. The same step kernel either way, so the same states.
     cuda_check(cudaMemsetAsync(sl, 0, state_bytes, s), "zero state");
+    int cur = 0;  // slot holding the current state
     for (int k = 0; k < n_ck; ++k) {
       const int s0 = k * C, s1 = std::min(nt, s0 + C);
-      copy(sl, ck + k * state_bytes);
-      slots_forward(s0, s1, true);
-      if (k + 1 < n_ck) copy(sl + (s1 - s0) * state_bytes, sl);
+      copy(sl + cur * state_bytes, ck + k * state_bytes);
+      if (k + 1 < n_ck) {
+        for (int n = s0; n < s1; ++n) {
+          step(n, cur, cur ^ 1, true);
+          cur ^= 1;
+        }
+      } else {
+        if (cur != 0) copy(sl + cur * state_bytes, sl);
+        slots_forward(s0, s1, true);
+      }
     }
     const size_t off = static_cast<size_t>(shot) * nr * nt;
     if (nr) {

@@ -295,7 +295,7 @@ class Model {
   DeviceBuffer gff_shots_;
   cudaEvent_t lanes_start_ = nullptr;
   static constexpr int kMaxLanes = 8;
-  static constexpr int kFlushSteps = 10;  // exact step: partial sums into the pairs
+  static constexpr int kFlushSteps = 20;  // exact step: partial sums into the pairs
   int exact_lane_count(int C, int n_list) const;
   size_t exact_lane_bytes(int C) const;
   double exact_gradient_lanes(int C, const std::vector<int> &shot_list);
