@@ -87,6 +87,15 @@ const char *psv_last_error(void);
 /* Number of CUDA devices visible; 0 when none. */
 int psv_device_count(int *count);
 
+/* Page-locked host memory (cudaMallocHost / cudaFreeHost). Getters that copy
+ * into it run at the host link's full rate instead of going through the
+ * driver's staging of pageable memory. No counterpart in the reference (its
+ * getters return fresh arrays, src/psvWave.cpp:33-63): psvwave_gb300.fdModel
+ * backs the large arrays its getters return with blocks from a pool of these,
+ * reused once an array is freed. */
+int psv_host_alloc(size_t bytes, void **ptr);
+int psv_host_free(void *ptr);
+
 /* Parses and validates a configuration file (the reference's INI reading,
  * src/fdModel.cpp:470-523, and checks, src/fdModel.cpp:390-468) without
  * touching a GPU; fills `out` with precision = device = -1 and misfit = 0. */

@@ -57,6 +57,8 @@ _SIGNATURES = {
     "psv_abi_version": [],
     "psv_last_error": [],
     "psv_device_count": [_ip],
+    "psv_host_alloc": [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)],
+    "psv_host_free": [_vp],
     "psv_config_info": [ctypes.c_char_p, ctypes.POINTER(PsvInfo)],
     "psv_create_from_ini": [ctypes.c_char_p, _c_int, _c_int, ctypes.POINTER(_vp)],
     "psv_create": [ctypes.POINTER(PsvParams), _c_int, _c_int, ctypes.POINTER(_vp)],

@@ -77,6 +77,31 @@ int psv_device_count(int *count) {
   });
 }
 
+int psv_host_alloc(size_t bytes, void **ptr) {
+  return guarded([&] {
+    need(ptr, "ptr");
+    *ptr = nullptr;
+    if (!bytes) return;
+    const cudaError_t e = cudaMallocHost(ptr, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      *ptr = nullptr;
+      throw psv::Error(PSV_ERR_CUDA, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+  });
+}
+
+int psv_host_free(void *ptr) {
+  return guarded([&] {
+    if (!ptr) return;
+    const cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw psv::Error(PSV_ERR_CUDA, std::string("cudaFreeHost: ") + cudaGetErrorString(e));
+    }
+  });
+}
+
 int psv_create_from_ini(const char *path, int precision, int device, psv_model **out) {
   return guarded([&] {
     need(path, "path");

@@ -8,6 +8,8 @@ the reference's getters do (src/psvWave.cpp:33-63). The extra keyword
 reference's own precision, bit-identical to it); `device` picks the GPU.
 """
 import ctypes
+import threading
+import weakref
 
 import numpy as np
 
@@ -20,8 +22,58 @@ def _ptr(a):
     return a.ctypes.data_as(_DP)
 
 
+class _PinnedPool:
+    """Page-locked host blocks (psv_host_alloc) behind the large arrays the
+    getters return. A device-to-host copy into page-locked memory runs at
+    the host link's rate; into a fresh pageable array it goes through the
+    driver's staging and first-touch page faults. A block returns to the
+    pool when the last array viewing it is freed, so a loop that reads
+    seismograms every iteration reuses the same blocks. Arrays below
+    MIN_BYTES, and any array once the pool holds MAX_BYTES, are plain numpy
+    arrays."""
+
+    MIN_BYTES = 1 << 20
+    MAX_BYTES = 4 << 30
+
+    def __init__(self):
+        self._free = {}
+        self._held = 0
+        self._lock = threading.Lock()
+        self._off = False  # set when the first allocation fails (no device)
+
+    def array(self, shape):
+        n = int(np.prod(shape)) * 8
+        if n < self.MIN_BYTES or self._off:
+            return np.empty(shape, dtype=np.float64)
+        ptr = None
+        with self._lock:
+            blocks = self._free.get(n)
+            if blocks:
+                ptr = blocks.pop()
+            elif self._held + n <= self.MAX_BYTES:
+                p = ctypes.c_void_p()
+                if _capi.load().psv_host_alloc(n, ctypes.byref(p)) == _capi.PSV_OK and p.value:
+                    ptr = p.value
+                    self._held += n
+                else:
+                    self._off = True
+        if ptr is None:
+            return np.empty(shape, dtype=np.float64)
+        buf = (ctypes.c_double * (n // 8)).from_address(ptr)
+        weakref.finalize(buf, self._release, n, ptr)
+        return np.frombuffer(buf, dtype=np.float64).reshape(shape)
+
+    def _release(self, n, ptr):
+        with self._lock:
+            self._free.setdefault(n, []).append(ptr)
+
+
+_PINNED = _PinnedPool()
+
+
 def _out(shape):
-    return np.empty(shape, dtype=np.float64)
+    """A fresh float64 array for a getter to fill (page-locked when large)."""
+    return _PINNED.array(shape)
 
 
 def _in(a, shape, name):
