@@ -141,6 +141,22 @@ cudaError_t copy_state(const void *const src[5], void *const dst[5], void *const
   return cudaGetLastError();
 }
 
+__global__ void add_into3_kernel(size_t n, const double *a0, const double *a1, const double *a2,
+                                 double *b0, double *b1, double *b2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    b0[i] += a0[i];
+    b1[i] += a1[i];
+    b2[i] += a2[i];
+  }
+}
+
+cudaError_t add_into3(size_t n, const double *const src[3], double *const dst[3], cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  add_into3_kernel<<<blocks_for(n), 256, 0, s>>>(n, src[0], src[1], src[2], dst[0], dst[1], dst[2]);
+  return cudaGetLastError();
+}
+
 cudaError_t exact_chain(size_t n, const double *vp, const double *vs, const double *rho,
                         const double *g_lm, const double *g_la, const double *g_mu,
                         const double *g_b, double *g_vp, double *g_vs, double *g_rho,

@@ -932,6 +932,32 @@ void Model::destroy_lanes() {
 // same whatever C. Each shot's pipeline is captured once as a CUDA graph on
 // its lane's stream and replayed. At the end the shots' sums are added in
 // shot order, and the chain rule maps them to (vp, vs, rho).
+int Model::ensure_lanes(int K) {
+  int changed = 0;
+  // Lanes beyond K give their memory back.
+  while (static_cast<int>(lanes_.size()) > K) {
+    auto &l = lanes_.back();
+    if (l->stream) {
+      cuda_check(cudaStreamSynchronize(l->stream), "lane sync");
+      cudaStreamDestroy(l->stream);
+    }
+    if (l->done) cudaEventDestroy(l->done);
+    lanes_.pop_back();
+    changed = 1;
+  }
+  while (static_cast<int>(lanes_.size()) < K) {
+    auto l = std::make_unique<ExactLane>();
+    if (!lanes_.empty())
+      cuda_check(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking), "lane stream");
+    cuda_check(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming), "lane event");
+    lanes_.push_back(std::move(l));
+    changed = 1;
+  }
+  if (!lanes_start_)
+    cuda_check(cudaEventCreateWithFlags(&lanes_start_, cudaEventDisableTiming), "lane event");
+  return changed;
+}
+
 double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
   const int nt = cfg_.nt, n_shots = cfg_.n_shots, nr = cfg_.nr;
   if (C <= 0 || C > nt) C = nt;
@@ -964,27 +990,7 @@ double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
       grown = true;
     }
   };
-  // Lanes beyond K give their memory back.
-  while (static_cast<int>(lanes_.size()) > K) {
-    auto &l = lanes_.back();
-    if (l->stream) {
-      cuda_check(cudaStreamSynchronize(l->stream), "lane sync");
-      cudaStreamDestroy(l->stream);
-    }
-    if (l->done) cudaEventDestroy(l->done);
-    lanes_.pop_back();
-    grown = true;
-  }
-  while (static_cast<int>(lanes_.size()) < K) {
-    auto l = std::make_unique<ExactLane>();
-    if (!lanes_.empty())
-      cuda_check(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking), "lane stream");
-    cuda_check(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming), "lane event");
-    lanes_.push_back(std::move(l));
-    grown = true;
-  }
-  if (!lanes_start_)
-    cuda_check(cudaEventCreateWithFlags(&lanes_start_, cudaEventDisableTiming), "lane event");
+  if (ensure_lanes(K)) grown = true;
   for (auto &l : lanes_) {
     ensure(l->ckpt, n_ck * state_bytes);
     ensure(l->slots, (C + 1) * state_bytes);
@@ -1233,6 +1239,164 @@ double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
   synchronize();
   check_device_error();
   return misfit;
+}
+
+bool Model::run_model_lanes_ok() const {
+  return prec_ == PSV_FP32 && tma_ok_ && cfg_.n_shots > 1 &&
+         (variant_ == kFusedTma || variant_ == kFusedTmaPersistent);
+}
+
+// run_model with the shots in concurrent lanes (FP32, per-step TMA
+// launches; the persistent scheme's steps are the same tile arithmetic, so
+// the same states). Forward phase: each shot, in lane k % K, advances from
+// zero fields in the lane's two state slots (ping-pong), storing its
+// snapshots and recording its receivers into the lane's raw series, then
+// its seismograms. The misfit and adjoint sources follow on the model's
+// stream. Adjoint phase: each shot's adjoint in its lane, correlating into
+// the shot's own kernel sums, which are added to the kernels in shot order.
+// The last shot's final fields are copied into the model's fields, where
+// the serial run leaves them.
+void Model::run_model_lanes(bool simulate_adjoint) {
+  DeviceGuard guard(device_);
+  ensure_snapshots();
+  const int n_shots = cfg_.n_shots, nr = cfg_.nr, nt = cfg_.nt;
+  const int K = std::min(n_shots, kMaxLanes);
+  const size_t gp = padded_size(), g = grid_size();
+  const size_t field_bytes = gp * sizeof(float), state_bytes = 5 * field_bytes;
+  cudaStream_t ms = stream();
+  bool grown = ensure_lanes(K) != 0;
+  auto ensure = [&](DeviceBuffer &b, size_t bytes) {
+    if (b.bytes() < bytes) {
+      synchronize();
+      for (auto &l : lanes_)
+        if (l->stream) cuda_check(cudaStreamSynchronize(l->stream), "lane sync");
+      b.allocate(bytes);
+      grown = true;
+    }
+  };
+  for (auto &l : lanes_) {
+    ensure(l->slots, 2 * state_bytes);
+    ensure(l->raw, std::max<size_t>(2 * static_cast<size_t>(nr) * nt * sizeof(float), 16));
+  }
+  ensure(kshots_, static_cast<size_t>(n_shots) * 3 * g * sizeof(double));
+  if (grown) clear_graphs();
+  auto slot_fields = [&](ExactLane &l, int j) {
+    float *b = reinterpret_cast<float *>(l.slots.as<unsigned char>() + j * state_bytes);
+    return fast::Fields{b, b + gp, b + 2 * gp, b + 3 * gp, b + 4 * gp};
+  };
+  for (auto &lp : lanes_) {
+    ExactLane &l = *lp;
+    if (l.rm_slots == l.slots.get() && l.rm_cfg == tile_cfg_) continue;
+    for (int j = 0; j < 2; ++j)
+      if (!tma::encode_input_maps(l.rm_maps[j], slot_fields(l, j), lm_.as<float>(),
+                                  mu_.as<float>(), geo_.nx, geo_.nz, pitch_, tile_cfg_))
+        throw Error(PSV_ERR_CUDA, "tensor-map encoding failed for a lane's state");
+    l.rm_slots = l.slots.get();
+    l.rm_cfg = tile_cfg_;
+  }
+  // One shot's forward (adjoint = false) or adjoint, in lane l on stream s.
+  auto one = [&](ExactLane &l, int shot, bool adjoint, cudaStream_t s) {
+    cuda_check(cudaMemsetAsync(l.slots.get(), 0, 2 * state_bytes, s), "zero state");
+    tma::SimDesc d = descs_h_[adjoint ? n_shots + shot : shot];
+    for (int j = 0; j < 2; ++j) {
+      d.set[j] = slot_fields(l, j);
+      d.maps[j] = l.rm_maps[j];
+    }
+    float *raw = l.raw.as<float>();
+    d.rec_vx = nr ? raw : nullptr;
+    d.rec_vz = nr ? raw + static_cast<size_t>(nr) * nt : nullptr;
+    if (adjoint) {
+      double *k = kshots_.as<double>() + static_cast<size_t>(shot) * 3 * g;
+      cuda_check(cudaMemsetAsync(k, 0, 3 * g * sizeof(double), s), "zero kernels");
+      d.klam = k;
+      d.kmu = k + g;
+      d.krho = k + 2 * g;
+    }
+    int cur = 0;
+    for (int n = 0; n < nt; ++n) {
+      const int it = adjoint ? nt - 1 - n : n;
+      cuda_check(tma::step_single(d, tile_cfg_, adjoint, it, cur, !adjoint, err_flag_.as<int>(), s),
+                 adjoint ? "adjoint_simulate" : "forward_simulate");
+      cur ^= 1;
+    }
+    if (!adjoint && nr) {
+      const size_t off = static_cast<size_t>(shot) * nr * nt;
+      cuda_check(receiver_cumsum_f32(nr, nt, nt, cfg_.dt, cfg_.dx * cfg_.dz, raw,
+                                     raw + static_cast<size_t>(nr) * nt,
+                                     rtf_[0].as<double>() + off, rtf_[1].as<double>() + off, s),
+                 "seismograms");
+    }
+  };
+  auto phase = [&](bool adjoint) {
+    cuda_check(cudaEventRecord(lanes_start_, ms), "lane start");
+    for (int k = 1; k < K; ++k)
+      cuda_check(cudaStreamWaitEvent(lanes_[k]->stream, lanes_start_, 0), "lane wait");
+    for (int shot = 0; shot < n_shots; ++shot) {
+      const int li = shot % K;
+      ExactLane &l = *lanes_[li];
+      cudaStream_t s = li == 0 ? ms : l.stream;
+      auto enqueue = [&] { one(l, shot, adjoint, s); };
+      if (!use_graphs_) {
+        enqueue();
+        continue;
+      }
+      GraphEntry &ge = graphs_[std::make_tuple(20 + li, shot, K, adjoint ? 1 : 0)];
+      if (ge.exec) {
+        cuda_check(cudaGraphLaunch(ge.exec, s), "cudaGraphLaunch");
+        continue;
+      }
+      if (ge.uses++ == 0) {
+        enqueue();
+        continue;
+      }
+      cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                 "cudaStreamBeginCapture");
+      try {
+        enqueue();
+      } catch (...) {
+        cudaGraph_t broken = nullptr;
+        cudaStreamEndCapture(s, &broken);
+        if (broken) cudaGraphDestroy(broken);
+        throw;
+      }
+      cudaGraph_t graph = nullptr;
+      cuda_check(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
+      cudaError_t e = cudaGraphInstantiate(&ge.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      cuda_check(e, "cudaGraphInstantiate");
+      cuda_check(cudaGraphLaunch(ge.exec, s), "cudaGraphLaunch");
+    }
+    for (int k = 1; k < K; ++k) {
+      cuda_check(cudaEventRecord(lanes_[k]->done, lanes_[k]->stream), "lane done");
+      cuda_check(cudaStreamWaitEvent(ms, lanes_[k]->done, 0), "lane join");
+    }
+    // The last shot's final state into the model's fields (nt steps from
+    // slot 0 end in slot nt % 2).
+    ExactLane &last = *lanes_[(n_shots - 1) % K];
+    void *src[5], *dst[5];
+    for (int f = 0; f < 5; ++f) {
+      src[f] = last.slots.as<unsigned char>() + (nt & 1) * state_bytes + f * field_bytes;
+      dst[f] = fields_[f].get();
+    }
+    cuda_check(copy_state(src, dst, nullptr, field_bytes, ms), "final state");
+    cur_ = 0;
+  };
+  phase(false);
+  calculate_l2_misfit();
+  if (simulate_adjoint) {
+    calculate_l2_adjoint_sources();
+    reset_kernels();
+    phase(true);
+    double *dst[3] = {klame_[0].as<double>(), klame_[1].as<double>(), klame_[2].as<double>()};
+    for (int shot = 0; shot < n_shots; ++shot) {
+      const double *k = kshots_.as<double>() + static_cast<size_t>(shot) * 3 * g;
+      const double *src[3] = {k, k + g, k + 2 * g};
+      cuda_check(add_into3(g, src, dst, ms), "kernel sums");
+    }
+    map_kernels_to_velocity();
+  }
+  synchronize();
+  check_device_error();
 }
 
 void Model::get_exact_gradient(double *g_vp, double *g_vs, double *g_rho, bool device_pointers) {
@@ -1668,6 +1832,10 @@ void Model::map_kernels_to_velocity() {
 }
 
 void Model::run_model(bool verbose, bool simulate_adjoint) {
+  if (!verbose && run_model_lanes_ok()) {
+    run_model_lanes(simulate_adjoint);
+    return;
+  }
   const bool was_async = async_;
   async_ = true;
   try {

@@ -290,7 +290,17 @@ class Model {
     const void *maps_slots = nullptr;  // slots / lam / C / tile shape the maps were made for
     const void *maps_lam = nullptr;
     int maps_C = -1, maps_cfg = -1;
+    tma::Maps rm_maps[2];               // run_model lanes: input maps of slots 0 and 1
+    const void *rm_slots = nullptr;
+    int rm_cfg = -1;
   };
+  // run_model in lanes (FP32, TMA per-step launches): every shot's forward
+  // with snapshots, then every shot's adjoint with kernel correlation into
+  // per-shot sums (kshots_), added in shot order.
+  DeviceBuffer kshots_;
+  bool run_model_lanes_ok() const;
+  void run_model_lanes(bool simulate_adjoint);
+  int ensure_lanes(int K);  // makes exactly K lanes; returns 1 when lanes were (re)made
   std::vector<std::unique_ptr<ExactLane>> lanes_;
   DeviceBuffer gff_shots_;
   cudaEvent_t lanes_start_ = nullptr;

@@ -150,6 +150,8 @@ cudaError_t map_kernels(size_t n, const double *vp, const double *vs, const doub
 // sum_{m >= n} dt (syn[r][m] - obs[r][m]), per receiver row of length nt.
 cudaError_t exact_receiver_terms(int rows, int nt, double dt, double dxdz, const double *syn,
                                  const double *obs, double *adj, cudaStream_t s);
+// dst[k][i] += src[k][i] for k < 3, i < n (FP64).
+cudaError_t add_into3(size_t n, const double *const src[3], double *const dst[3], cudaStream_t s);
 // Copies five wave-field arrays of `bytes` each (a multiple of 16, all
 // pointers 16-byte aligned) from src[f] to dst[f], and to dst2[f] too when
 // dst2 is non-null: one launch for a whole state.

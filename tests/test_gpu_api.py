@@ -254,3 +254,71 @@ def test_mid_grid_defaults_to_small_tiles():
     m = psv.fdModel.from_parameters(workloads.c3_params(nt=10, n_shots=1))
     assert m.kernel_variant == "fused_tma"
     assert m.tile_shape == "16x28"
+
+
+def test_returned_arrays_are_independent_copies():
+    """Getters return fresh arrays (src/psvWave.cpp:33-63) even though large
+    ones are backed by pooled page-locked blocks: an array still held keeps
+    its block, so later calls never write into it; a freed array's block is
+    reused."""
+    p = small_params()
+    p.update(nt=10000)  # 2 shots x 7 receivers x 10000 steps x 8 B = 1.1 MB per component
+    m = psv.fdModel.from_parameters(p, precision="fp64")
+    big = m.get_lame_kernels()  # kernels: small grids stay plain numpy arrays
+    m.forward_simulate(0, False)
+    first = m.get_synthetic_data()
+    keep = [a.copy() for a in first]
+    m.set_parameter_fields(*(a * 1.01 for a in m.get_parameter_fields()))
+    m.forward_simulate(0, False)
+    second = m.get_synthetic_data()
+    for a, k in zip(first, keep):
+        assert np.array_equal(a, k)
+    assert not np.array_equal(first[0], second[0])
+    assert big[0].shape == (m.nx, m.nz)
+
+
+def test_pinned_pool_reuses_freed_blocks():
+    from psvwave_gb300 import model as model_module
+
+    pool = model_module._PINNED
+    shape = (256, 1024)  # 2 MB: taken from the pool
+    a = pool.array(shape)
+    a[...] = 1.0
+    b = pool.array(shape)
+    assert a.ctypes.data != b.ctypes.data
+    addr = a.ctypes.data
+    del a
+    import gc
+
+    gc.collect()
+    c = pool.array(shape)
+    assert c.ctypes.data == addr
+    assert b.ctypes.data != c.ctypes.data
+
+
+@pytest.mark.parametrize("variant", ["fused_tma", "fused_tma_persistent"])
+def test_fp32_run_model_lanes_equal_serial_calls(golden, variant):
+    """FP32 run_model runs its shots in concurrent lanes (per-shot kernel sums
+    added in shot order); the serial forward_simulate / adjoint_simulate
+    calls give the same seismograms, misfit and final wave fields bit for
+    bit, and the same kernels up to the order of their FP64 sums."""
+    a = psv.fdModel(SMALL_INI, precision="fp32")
+    b = psv.fdModel(SMALL_INI, precision="fp32")
+    for m in (a, b):
+        m.kernel_variant = variant
+    fwi_gradient(a, tuple(golden["target"]), tuple(golden["start"]))
+    b.set_parameter_fields(*golden["target"])
+    for s in range(b.n_shots):
+        b.forward_simulate(s, False)
+    b.set_observed_data(*b.get_synthetic_data())
+    b.set_parameter_fields(*golden["start"])
+    for _ in range(3):  # eager, graph capture, graph replay
+        b.run_model(False, True)
+        assert a.misfit == b.misfit
+        for x, y in zip(a.get_synthetic_data(), b.get_synthetic_data()):
+            assert np.array_equal(x, y)
+        for x, y in zip(a.get_wavefields(), b.get_wavefields()):
+            assert np.array_equal(x, y)
+        for x, y in zip(a.get_lame_kernels(), b.get_lame_kernels()):
+            assert rel_l2(y, x) <= 1e-12
+        assert rel_l2(b.get_gradient_vector(), a.get_gradient_vector()) <= 1e-12
