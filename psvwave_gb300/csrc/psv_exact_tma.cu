@@ -80,9 +80,8 @@ constexpr int TOTAL = OFF_W + 2 * VB;
 // later holds p_z).
 constexpr int TX_BYTES = (OFF_W - SB) * 4;
 constexpr int SMEM = TOTAL * 4 + 16 + 128;  // + mbarrier + alignment slack
-constexpr int ROWS = TX / (NT / 32);        // own rows per thread
 static_assert((VB * 4) % 128 == 0 && (SB * 4) % 128 == 0, "boxes must stay 128-byte aligned");
-static_assert(TZ == 32 && TX % (NT / 32) == 0, "one warp per tile row");
+static_assert(TZ == 32 && TX * TZ == 2 * NT, "a pair of own points per thread");
 
 __device__ __forceinline__ float taper_at(const Step &a, int ix, int iz) {
   int c = min(min(ix + 1, iz + 1), min(a.nx - ix, a.nz - iz));
@@ -102,35 +101,72 @@ __device__ __forceinline__ float2 ff_add(float2 a, float x) {
   return make_float2(s, a.y + e);
 }
 
+__device__ __forceinline__ float2 ld2(const float *p) {
+  return *reinterpret_cast<const float2 *>(p);
+}
+__device__ __forceinline__ void st2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
+
+// Staggered differences of a pair of adjacent points k, k + 1 (k even) from
+// three float2 loads of their row, L = [k-2, k-1], C = [k, k+1],
+// R = [k+2, k+3], with folded coefficients a1 = c1 / h, a2 = c2 / h:
+// backward D- f(k) = a1 (f[k] - f[k-1]) + a2 (f[k-2] - f[k+1]),
+// forward  D+ f(k) = a1 (f[k+1] - f[k]) + a2 (f[k-1] - f[k+2]).
+__device__ __forceinline__ float2 dm_pair(float2 L, float2 C, float2 R, float a1, float a2) {
+  return make_float2(a1 * (C.x - L.y) + a2 * (L.x - C.y), a1 * (C.y - C.x) + a2 * (L.y - R.x));
+}
+__device__ __forceinline__ float2 dp_pair(float2 L, float2 C, float2 R, float a1, float a2) {
+  return make_float2(a1 * (C.y - C.x) + a2 * (L.y - R.x), a1 * (R.x - C.y) + a2 * (C.x - R.y));
+}
+// The same along x from the pair's values in rows -2, -1, 0, +1, +2 (m2 ..
+// p2; a row a formula does not use may be anything).
+__device__ __forceinline__ float2 dxm_pair(float2 m2, float2 m1, float2 c0, float2 p1, float a1,
+                                           float a2) {
+  return make_float2(a1 * (c0.x - m1.x) + a2 * (m2.x - p1.x), a1 * (c0.y - m1.y) + a2 * (m2.y - p1.y));
+}
+__device__ __forceinline__ float2 dxp_pair(float2 m1, float2 c0, float2 p1, float2 p2, float a1,
+                                           float a2) {
+  return make_float2(a1 * (p1.x - c0.x) + a2 * (m1.x - p2.x), a1 * (p1.y - c0.y) + a2 * (m1.y - p2.y));
+}
+
 // Phases 1-3 of one tile (the copies have landed). INNER: every point of
 // the 4-halo region is interior with taper 1 and no own point has a source
-// term.
+// term. Phases 2 and 3 give each thread a pair of adjacent z columns: every
+// shared-memory access is a float2, and the z-direction stencils of the two
+// points share their loads. The difference coefficients are folded with
+// 1/dx and 1/dz. Phase 3: thread t owns points (X0 + t / 16,
+// Z0 + 2 (t % 16) + {0, 1}); gpart[q] are their partial sums.
 template <bool INNER>
 __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int Z0,
-                                          const float2 *glm, const float2 *gla,
-                                          const float2 *gmu, const float2 *gb,
                                           const float4 *gpart) {
-  const int tid = threadIdx.x, lane = tid & 31, wr = tid >> 5;
-  const int iz = Z0 + lane;
+  const int tid = threadIdx.x;
   const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
+  const float c1x = c1 * a.idx, c2x = c2 * a.idx, c1z = c1 * a.idz, c2z = c2 * a.idz;
   const float *LVX = sm + OFF_LV, *LVZ = sm + OFF_LV + VB, *B = sm + OFF_B;
   float *WX = sm + OFF_W, *WZ = sm + OFF_W + VB;
   // Phase 1: w = b dt T lv at interior points, 0 elsewhere.
-  for (int k = tid; k < VB; k += NT) {
-    const int r = k / W, c = k - r * W;
-    const int ix = X0 - 4 + r, jz = Z0 - 4 + c;
-    float wx = 0.f, wz = 0.f;
-    if (INNER) {
-      const float s = B[k] * a.dt;
-      wx = s * LVX[k];
-      wz = s * LVZ[k];
-    } else if (ix >= 0 && ix < a.nx && jz >= 0 && jz < a.nz && interior(a, ix, jz)) {
-      const float s = B[k] * a.dt * taper_at(a, ix, jz);
-      wx = s * LVX[k];
-      wz = s * LVZ[k];
+  if (INNER) {
+    static_assert(VB % 4 == 0 && VB / 4 <= NT, "one float4 of the 4-halo box per thread");
+    if (tid < VB / 4) {
+      const float4 b4 = reinterpret_cast<const float4 *>(B)[tid];
+      const float4 x4 = reinterpret_cast<const float4 *>(LVX)[tid];
+      const float4 z4 = reinterpret_cast<const float4 *>(LVZ)[tid];
+      const float s0 = b4.x * a.dt, s1 = b4.y * a.dt, s2 = b4.z * a.dt, s3 = b4.w * a.dt;
+      reinterpret_cast<float4 *>(WX)[tid] = make_float4(s0 * x4.x, s1 * x4.y, s2 * x4.z, s3 * x4.w);
+      reinterpret_cast<float4 *>(WZ)[tid] = make_float4(s0 * z4.x, s1 * z4.y, s2 * z4.z, s3 * z4.w);
     }
-    WX[k] = wx;
-    WZ[k] = wz;
+  } else {
+    for (int k = tid; k < VB; k += NT) {
+      const int r = k / W, c = k - r * W;
+      const int ix = X0 - 4 + r, jz = Z0 - 4 + c;
+      float wx = 0.f, wz = 0.f;
+      if (ix >= 0 && ix < a.nx && jz >= 0 && jz < a.nz && interior(a, ix, jz)) {
+        const float s = B[k] * a.dt * taper_at(a, ix, jz);
+        wx = s * LVX[k];
+        wz = s * LVZ[k];
+      }
+      WX[k] = wx;
+      WZ[k] = wz;
+    }
   }
   __syncthreads();
 
@@ -139,130 +175,197 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
   float *PX = sm + OFF_P, *PZ = sm + OFF_P + SB, *QQ = sm + OFF_P + 2 * SB;
   // Phase 2: lt~ = lt - (A^T w terms), and p_x = dt (lm y_xx + la y_zz),
   // p_z = dt (la y_xx + lm y_zz), q = dt mu y_xz with y = T lt~ on I, 0
-  // elsewhere; over rows X0-2 .. X0+TX+1 and columns Z0-2 .. Z0+TZ+1.
-  for (int k = tid; k < SR * PC; k += NT) {
-    const int r = k / PC, c = 2 + (k - r * PC);
+  // elsewhere; over rows X0-2 .. X0+TX+1 and columns Z0-2 .. Z0+TZ+1, a
+  // pair of columns per thread and round.
+  constexpr int PP = PC / 2;  // column pairs per row
+  for (int k = tid; k < SR * PP; k += NT) {
+    const int r = k / PP, c = 2 + 2 * (k - r * PP);
     const int ix = X0 - 2 + r, jz = Z0 - 4 + c;
     const int s = r * W + c;        // in the 2-halo boxes
-    const int v = (r + 2) * W + c;  // the same point in the 4-halo boxes
-    float px = 0.f, pz = 0.f, q = 0.f;
-    if (INNER || (ix >= 0 && ix < a.nx && jz >= 0 && jz < a.nz)) {
-      const float dxp_wx = c1 * (WX[v + W] - WX[v]) + c2 * (WX[v - W] - WX[v + 2 * W]);
-      const float dzp_wx = c1 * (WX[v + 1] - WX[v]) + c2 * (WX[v - 1] - WX[v + 2]);
-      const float dzm_wz = c1 * (WZ[v] - WZ[v - 1]) + c2 * (WZ[v - 2] - WZ[v + 1]);
-      const float dxm_wz = c1 * (WZ[v] - WZ[v - W]) + c2 * (WZ[v - 2 * W] - WZ[v + W]);
-      const float lxx = LXX[s] - dxp_wx * a.idx;
-      const float lzz = LZZ[s] - dzm_wz * a.idz;
-      const float lxz = LXZ[s] - dzp_wx * a.idz - dxm_wz * a.idx;
-      LXX[s] = lxx;
-      LZZ[s] = lzz;
-      LXZ[s] = lxz;
-      if (INNER) {
-        const float lm = LM[s], mu = MU[s];
-        const float la = lm - 2.0f * mu;
-        px = a.dt * (lm * lxx + la * lzz);
-        pz = a.dt * (la * lxx + lm * lzz);
-        q = a.dt * mu * lxz;
-      } else if (interior(a, ix, jz)) {
-        const float tp = taper_at(a, ix, jz);
-        const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
-        if (!(yxx == 0.f && yzz == 0.f && yxz == 0.f)) {
-          const float lm = LM[s], mu = MU[s];
-          const float la = lm - 2.0f * mu;
-          px = a.dt * (lm * yxx + la * yzz);
-          pz = a.dt * (la * yxx + lm * yzz);
-          q = a.dt * mu * yxz;
+    const int v = (r + 2) * W + c;  // the same points in the 4-halo boxes
+    const float2 wxm1 = ld2(WX + v - W), wx0 = ld2(WX + v), wxp1 = ld2(WX + v + W),
+                 wxp2 = ld2(WX + v + 2 * W), wxl = ld2(WX + v - 2), wxr = ld2(WX + v + 2);
+    const float2 wzm2 = ld2(WZ + v - 2 * W), wzm1 = ld2(WZ + v - W), wz0 = ld2(WZ + v),
+                 wzp1 = ld2(WZ + v + W), wzl = ld2(WZ + v - 2), wzr = ld2(WZ + v + 2);
+    const float2 dxp_wx = dxp_pair(wxm1, wx0, wxp1, wxp2, c1x, c2x);
+    const float2 dzp_wx = dp_pair(wxl, wx0, wxr, c1z, c2z);
+    const float2 dzm_wz = dm_pair(wzl, wz0, wzr, c1z, c2z);
+    const float2 dxm_wz = dxm_pair(wzm2, wzm1, wz0, wzp1, c1x, c2x);
+    const float2 oxx = ld2(LXX + s), ozz = ld2(LZZ + s), oxz = ld2(LXZ + s);
+    float2 lxx = make_float2(oxx.x - dxp_wx.x, oxx.y - dxp_wx.y);
+    float2 lzz = make_float2(ozz.x - dzm_wz.x, ozz.y - dzm_wz.y);
+    float2 lxz = make_float2(oxz.x - dzp_wx.x - dxm_wz.x, oxz.y - dzp_wx.y - dxm_wz.y);
+    const float2 lm = ld2(LM + s), mu = ld2(MU + s);
+    float2 px, pz, q;
+    if (INNER) {
+      const float la0 = lm.x - 2.0f * mu.x, la1 = lm.y - 2.0f * mu.y;
+      px = make_float2(a.dt * (lm.x * lxx.x + la0 * lzz.x), a.dt * (lm.y * lxx.y + la1 * lzz.y));
+      pz = make_float2(a.dt * (la0 * lxx.x + lm.x * lzz.x), a.dt * (la1 * lxx.y + lm.y * lzz.y));
+      q = make_float2(a.dt * mu.x * lxz.x, a.dt * mu.y * lxz.y);
+    } else {
+      float pxv[2] = {0.f, 0.f}, pzv[2] = {0.f, 0.f}, qv[2] = {0.f, 0.f};
+      float lxxv[2] = {lxx.x, lxx.y}, lzzv[2] = {lzz.x, lzz.y}, lxzv[2] = {lxz.x, lxz.y};
+      const float oxxv[2] = {oxx.x, oxx.y}, ozzv[2] = {ozz.x, ozz.y}, oxzv[2] = {oxz.x, oxz.y};
+      const float lmv[2] = {lm.x, lm.y}, muv[2] = {mu.x, mu.y};
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int j = jz + e;
+        if (!(ix >= 0 && ix < a.nx && j >= 0 && j < a.nz)) {
+          lxxv[e] = oxxv[e];  // outside the grid: lt~ is not formed there
+          lzzv[e] = ozzv[e];
+          lxzv[e] = oxzv[e];
+          continue;
+        }
+        if (interior(a, ix, j)) {
+          const float tp = taper_at(a, ix, j);
+          const float yxx = tp * lxxv[e], yzz = tp * lzzv[e], yxz = tp * lxzv[e];
+          if (!(yxx == 0.f && yzz == 0.f && yxz == 0.f)) {
+            const float la = lmv[e] - 2.0f * muv[e];
+            pxv[e] = a.dt * (lmv[e] * yxx + la * yzz);
+            pzv[e] = a.dt * (la * yxx + lmv[e] * yzz);
+            qv[e] = a.dt * muv[e] * yxz;
+          }
         }
       }
+      lxx = make_float2(lxxv[0], lxxv[1]);
+      lzz = make_float2(lzzv[0], lzzv[1]);
+      lxz = make_float2(lxzv[0], lxzv[1]);
+      px = make_float2(pxv[0], pxv[1]);
+      pz = make_float2(pzv[0], pzv[1]);
+      q = make_float2(qv[0], qv[1]);
     }
-    PX[s] = px;
-    PZ[s] = pz;
-    QQ[s] = q;
+    st2(LXX + s, lxx);
+    st2(LZZ + s, lzz);
+    st2(LXZ + s, lxz);
+    st2(PX + s, px);
+    st2(PZ + s, pz);
+    st2(QQ + s, q);
   }
   __syncthreads();
 
-  // Phase 3: own points.
-  if (!INNER && iz >= a.nz) return;
+  // Phase 3: own points, a pair per thread.
+  const int lx = tid >> 4, c = 4 + 2 * (tid & 15);
+  const int ix = X0 + lx, iz = Z0 + c - 4;
+  if (!INNER && (ix >= a.nx || iz >= a.nz)) return;
   const float *FVX = sm + OFF_FV, *FVZ = sm + OFF_FV + SB;
   const float *FXX = sm + OFF_FT, *FZZ = sm + OFF_FT + SB, *FXZ = sm + OFF_FT + 2 * SB;
   const int tile = blockIdx.x;
   const int r0 = a.rec_start[tile], r1 = a.rec_start[tile + 1];
-  const int c = lane + 4;
+  const int s = (lx + 2) * W + c;  // 2-halo boxes
+  const int v = (lx + 4) * W + c;  // 4-halo boxes
+  const float2 lxx = ld2(LXX + s), lzz = ld2(LZZ + s), lxz = ld2(LXZ + s);
+  const float2 lvx = ld2(LVX + v), lvz = ld2(LVZ + v);
+  const bool part = a.g_part != nullptr;
+  const float lxxv[2] = {lxx.x, lxx.y}, lzzv[2] = {lzz.x, lzz.y}, lxzv[2] = {lxz.x, lxz.y};
+  const float lvxv[2] = {lvx.x, lvx.y}, lvzv[2] = {lvz.x, lvz.y};
+  // Per point: inside the grid, interior, taper.
+  bool validv[2], inv[2];
+  float tpv[2];
 #pragma unroll
-  for (int j = 0; j < ROWS; ++j) {
-    const int lx = wr + j * (NT / 32);
-    const int ix = X0 + lx;
-    if (!INNER && ix >= a.nx) break;
-    const size_t p = (size_t)ix * a.pitch + iz;
-    const size_t u = (size_t)ix * a.nz + iz;
-    const int s = (lx + 2) * W + c;  // 2-halo boxes
-    const int v = (lx + 4) * W + c;  // 4-halo boxes
-    const bool in = INNER || interior(a, ix, iz);
-    const float tp = (INNER || !in) ? 1.f : taper_at(a, ix, iz);
-    const float lxx = LXX[s], lzz = LZZ[s], lxz = LXZ[s];
-    // tau-bar^n
-    a.olt[0][p] = tp * lxx;
-    a.olt[1][p] = tp * lzz;
-    a.olt[2][p] = tp * lxz;
-    // E^T (dt C y):  v-bar_x += -D-_x(p_x)/dx - D-_z(q)/dz,
-    //                v-bar_z += -D+_z(p_z)/dz - D+_x(q)/dx
-    const float dxm_px = c1 * (PX[s] - PX[s - W]) + c2 * (PX[s - 2 * W] - PX[s + W]);
-    const float dzm_q = c1 * (QQ[s] - QQ[s - 1]) + c2 * (QQ[s - 2] - QQ[s + 1]);
-    const float dzp_pz = c1 * (PZ[s + 1] - PZ[s]) + c2 * (PZ[s - 1] - PZ[s + 2]);
-    const float dxp_q = c1 * (QQ[s + W] - QQ[s]) + c2 * (QQ[s - W] - QQ[s + 2 * W]);
-    const float lvx = LVX[v], lvz = LVZ[v];
-    float ovx = tp * lvx - dxm_px * a.idx - dzm_q * a.idz;
-    float ovz = tp * lvz - dzp_pz * a.idz - dxp_q * a.idx;
+  for (int e = 0; e < 2; ++e) {
+    validv[e] = INNER || iz + e < a.nz;
+    inv[e] = INNER || (validv[e] && interior(a, ix, iz + e));
+    tpv[e] = (INNER || !inv[e]) ? 1.f : taper_at(a, ix, iz + e);
+  }
+  const size_t p0 = (size_t)ix * a.pitch + iz;
+  const bool both = INNER || iz + 1 < a.nz;
+  // Stage 1: the adjoint state. tau-bar^n = T lt~;
+  // E^T (dt C y):  v-bar_x += -D-_x(p_x)/dx - D-_z(q)/dz,
+  //                v-bar_z += -D+_z(p_z)/dz - D+_x(q)/dx
+  {
+    const float2 dxm_px = dxm_pair(ld2(PX + s - 2 * W), ld2(PX + s - W), ld2(PX + s),
+                                   ld2(PX + s + W), c1x, c2x);
+    const float2 q0 = ld2(QQ + s);
+    const float2 dzm_q = dm_pair(ld2(QQ + s - 2), q0, ld2(QQ + s + 2), c1z, c2z);
+    const float2 dxp_q =
+        dxp_pair(ld2(QQ + s - W), q0, ld2(QQ + s + W), ld2(QQ + s + 2 * W), c1x, c2x);
+    const float2 dzp_pz = dp_pair(ld2(PZ + s - 2), ld2(PZ + s), ld2(PZ + s + 2), c1z, c2z);
+    float ovx[2] = {tpv[0] * lvx.x - dxm_px.x - dzm_q.x, tpv[1] * lvx.y - dxm_px.y - dzm_q.y};
+    float ovz[2] = {tpv[0] * lvz.x - dzp_pz.x - dxp_q.x, tpv[1] * lvz.y - dzp_pz.y - dxp_q.y};
     // Receiver terms v-bar^n(rec) += adj[r][n].
     for (int i = r0; i < r1; ++i) {
       const int rr = a.rec_list[i];
-      if (a.rec_cell[rr] == (int)p) {
-        ovx = ovx + (float)a.adj_x[(size_t)rr * a.nt + a.it];
-        ovz = ovz + (float)a.adj_z[(size_t)rr * a.nt + a.it];
-      }
+      const int cell = a.rec_cell[rr];
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+        if (cell == (int)(p0 + e)) {
+          ovx[e] = ovx[e] + (float)a.adj_x[(size_t)rr * a.nt + a.it];
+          ovz[e] = ovz[e] + (float)a.adj_z[(size_t)rr * a.nt + a.it];
+        }
     }
-    a.olv[0][p] = ovx;
-    a.olv[1][p] = ovz;
-    float2 g_b = gb[j];
-    // With partial sums (a.g_part): this step's terms go into the FP32
-    // partial of the point (lm, la, mu, b); on a flush step the partial plus
-    // the terms go into the float-float pairs and the partial restarts at 0.
-    const bool part = a.g_part != nullptr;
-    float4 gq = gpart[j];
+    if (both) {
+      st2(a.olt[0] + p0, make_float2(tpv[0] * lxx.x, tpv[1] * lxx.y));
+      st2(a.olt[1] + p0, make_float2(tpv[0] * lzz.x, tpv[1] * lzz.y));
+      st2(a.olt[2] + p0, make_float2(tpv[0] * lxz.x, tpv[1] * lxz.y));
+      st2(a.olv[0] + p0, make_float2(ovx[0], ovx[1]));
+      st2(a.olv[1] + p0, make_float2(ovz[0], ovz[1]));
+    } else {
+      a.olt[0][p0] = tpv[0] * lxx.x;
+      a.olt[1][p0] = tpv[0] * lzz.x;
+      a.olt[2][p0] = tpv[0] * lxz.x;
+      a.olv[0][p0] = ovx[0];
+      a.olv[1][p0] = ovz[0];
+    }
+  }
+  // Stage 2: the gradient terms: grad_b += dt T lv . A tau^{n+1}, medium
+  // gradients from the strain rates of v^n.
+  const float2 fxz0 = ld2(FXZ + s);
+  const float2 ax_x = dxm_pair(ld2(FXX + s - 2 * W), ld2(FXX + s - W), ld2(FXX + s),
+                               ld2(FXX + s + W), c1x, c2x);
+  const float2 ax_z = dm_pair(ld2(FXZ + s - 2), fxz0, ld2(FXZ + s + 2), c1z, c2z);
+  const float2 az_x = dxp_pair(ld2(FXZ + s - W), fxz0, ld2(FXZ + s + W), ld2(FXZ + s + 2 * W),
+                               c1x, c2x);
+  const float2 az_z = dp_pair(ld2(FZZ + s - 2), ld2(FZZ + s), ld2(FZZ + s + 2), c1z, c2z);
+  const float axv[2] = {ax_x.x + ax_z.x, ax_x.y + ax_z.y};
+  const float azv[2] = {az_x.x + az_z.x, az_x.y + az_z.y};
+  const float2 fvx0 = ld2(FVX + s), fvz0 = ld2(FVZ + s);
+  const float2 ex = dxp_pair(ld2(FVX + s - W), fvx0, ld2(FVX + s + W), ld2(FVX + s + 2 * W), c1x,
+                             c2x);
+  const float2 gxz_x = dp_pair(ld2(FVX + s - 2), fvx0, ld2(FVX + s + 2), c1z, c2z);
+  const float2 ez = dm_pair(ld2(FVZ + s - 2), fvz0, ld2(FVZ + s + 2), c1z, c2z);
+  const float2 gxz_z = dxm_pair(ld2(FVZ + s - 2 * W), ld2(FVZ + s - W), fvz0, ld2(FVZ + s + W),
+                                c1x, c2x);
+  const float exv[2] = {ex.x, ex.y}, ezv[2] = {ez.x, ez.y};
+  const float gxzv[2] = {gxz_x.x + gxz_z.x, gxz_x.y + gxz_z.y};
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    if (!validv[e]) continue;
+    const int jz = iz + e;
+    const size_t u = (size_t)ix * a.nz + jz;
+    const float tp = tpv[e];
+    // The float-float pairs, where this step adds into them.
+    float2 glm = make_float2(0.f, 0.f), gla = glm, gmu = glm, g_b = glm;
+    if (!part || a.flush) {
+      glm = a.g_lm[u];
+      gla = a.g_la[u];
+      gmu = a.g_mu[u];
+      g_b = a.g_b[u];
+    }
+    float4 gq = gpart[e];
     float t_lm = 0.f, t_la = 0.f, t_mu = 0.f, t_b = 0.f;
-    if (in) {
-      // grad_b += dt T lv . A tau^{n+1}
-      const float ax = (c1 * (FXX[s] - FXX[s - W]) + c2 * (FXX[s - 2 * W] - FXX[s + W])) * a.idx +
-                       (c1 * (FXZ[s] - FXZ[s - 1]) + c2 * (FXZ[s - 2] - FXZ[s + 1])) * a.idz;
-      const float az = (c1 * (FXZ[s + W] - FXZ[s]) + c2 * (FXZ[s - W] - FXZ[s + 2 * W])) * a.idx +
-                       (c1 * (FZZ[s + 1] - FZZ[s]) + c2 * (FZZ[s - 1] - FZZ[s + 2])) * a.idz;
-      t_b = (a.dt * tp) * (lvx * ax + lvz * az);
-      if (!part) g_b = ff_add(g_b, t_b);
-      // Medium gradients from the strain rates of v^n.
-      const float ex = (c1 * (FVX[s + W] - FVX[s]) + c2 * (FVX[s - W] - FVX[s + 2 * W])) * a.idx;
-      const float ez = (c1 * (FVZ[s] - FVZ[s - 1]) + c2 * (FVZ[s - 2] - FVZ[s + 1])) * a.idz;
-      const float gxz = (c1 * (FVX[s + 1] - FVX[s]) + c2 * (FVX[s - 1] - FVX[s + 2])) * a.idz +
-                        (c1 * (FVZ[s] - FVZ[s - W]) + c2 * (FVZ[s - 2 * W] - FVZ[s + W])) * a.idx;
-      const float yxx = tp * lxx, yzz = tp * lzz, yxz = tp * lxz;
-      t_lm = a.dt * (yxx * ex + yzz * ez);
-      t_la = a.dt * (yxx * ez + yzz * ex);
-      t_mu = a.dt * yxz * gxz;
+    if (inv[e]) {
+      t_b = (a.dt * tp) * (lvxv[e] * axv[e] + lvzv[e] * azv[e]);
+      const float yxx = tp * lxxv[e], yzz = tp * lzzv[e], yxz = tp * lxzv[e];
+      t_lm = a.dt * (yxx * exv[e] + yzz * ezv[e]);
+      t_la = a.dt * (yxx * ezv[e] + yzz * exv[e]);
+      t_mu = a.dt * yxz * gxzv[e];
       if (!part) {
-        a.g_lm[u] = ff_add(glm[j], t_lm);
-        a.g_la[u] = ff_add(gla[j], t_la);
-        a.g_mu[u] = ff_add(gmu[j], t_mu);
+        g_b = ff_add(g_b, t_b);
+        a.g_lm[u] = ff_add(glm, t_lm);
+        a.g_la[u] = ff_add(gla, t_la);
+        a.g_mu[u] = ff_add(gmu, t_mu);
       }
     }
     // Source terms s = coef stf dt b / div at their points depend on b.
     const InjPlan &pl = a.plan;
     bool src = false;
-    if (!INNER && pl.n && ix >= pl.x0 && ix < pl.x0 + pl.w && iz >= pl.z0 && iz < pl.z0 + pl.h) {
-      int k = pl.map[(ix - pl.x0) * pl.h + (iz - pl.z0)];
+    if (!INNER && pl.n && ix >= pl.x0 && ix < pl.x0 + pl.w && jz >= pl.z0 && jz < pl.z0 + pl.h) {
+      int k = pl.map[(ix - pl.x0) * pl.h + (jz - pl.z0)];
       for (; k >= 0 && k < pl.n && pl.terms[k].cell == (int)u; ++k) {
         const InjTerm t = pl.terms[k];
         if (t.kind != 0) continue;
         const double ds = ((t.coef * a.stf[(size_t)t.index * a.nt + a.it]) * a.dt_d) / t.div;
-        const float ts = (float)(ds * (double)(t.field == 0 ? lvx : lvz));
+        const float ts = (float)(ds * (double)(t.field == 0 ? lvxv[e] : lvzv[e]));
         if (part)
           t_b += ts;
         else
@@ -271,7 +374,7 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
       }
     }
     if (!part) {
-      if (in || src) a.g_b[u] = g_b;
+      if (inv[e] || src) a.g_b[u] = g_b;
       continue;
     }
     gq.x += t_lm;
@@ -279,12 +382,12 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
     gq.z += t_mu;
     gq.w += t_b;
     if (a.flush) {
-      a.g_lm[u] = ff_add(glm[j], gq.x);
-      a.g_la[u] = ff_add(gla[j], gq.y);
-      a.g_mu[u] = ff_add(gmu[j], gq.z);
+      a.g_lm[u] = ff_add(glm, gq.x);
+      a.g_la[u] = ff_add(gla, gq.y);
+      a.g_mu[u] = ff_add(gmu, gq.z);
       a.g_b[u] = ff_add(g_b, gq.w);
       a.g_part[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-    } else if (in || src) {
+    } else if (inv[e] || src) {
       a.g_part[u] = gq;
     }
   }
@@ -325,29 +428,18 @@ __global__ void __launch_bounds__(NT, 4)
   }
   griddep_launch_dependents();
 
-  // This thread's own points (column lane, rows w, w + 8, ...) and their
-  // gradient sums, loaded while the copies fly.
-  const int lane = tid & 31, wr = tid >> 5;
-  const int iz = Z0 + lane;
+  // This thread's own points (row X0 + tid / 16, columns Z0 + 2 (tid % 16)
+  // + {0, 1}) and their gradient sums, loaded while the copies fly.
   // (With partial sums, the pairs are read only on flush steps.)
-  float2 glm[ROWS], gla[ROWS], gmu[ROWS], gb[ROWS];
-  float4 gpart[ROWS];
-  const bool pairs = a.g_part == nullptr || a.flush;
+  // (The float-float pairs are read in phase 3, where they are needed:
+  // every step without partial sums, flush steps with them.)
+  float4 gpart[2];
+  const int own_x = X0 + (tid >> 4), own_z = Z0 + 2 * (tid & 15);
 #pragma unroll
-  for (int j = 0; j < ROWS; ++j) {
-    const int ix = X0 + wr + j * (NT / 32);
-    glm[j] = gla[j] = gmu[j] = gb[j] = make_float2(0.f, 0.f);
+  for (int j = 0; j < 2; ++j) {
+    const int ix = own_x, iz = own_z + j;
     gpart[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (ix < a.nx && iz < a.nz) {
-      const size_t u = (size_t)ix * a.nz + iz;
-      if (pairs) {
-        glm[j] = a.g_lm[u];
-        gla[j] = a.g_la[u];
-        gmu[j] = a.g_mu[u];
-        gb[j] = a.g_b[u];
-      }
-      if (a.g_part) gpart[j] = a.g_part[u];
-    }
+    if (a.g_part && ix < a.nx && iz < a.nz) gpart[j] = a.g_part[(size_t)ix * a.nz + iz];
   }
 
   const bool landed = mbar_wait(bar, 0, 1u << 20);
@@ -367,9 +459,9 @@ __global__ void __launch_bounds__(NT, 4)
                      !(pl.n && X0 < pl.x0 + pl.w && pl.x0 < X0 + TX && Z0 < pl.z0 + pl.h &&
                        pl.z0 < Z0 + TZ);
   if (inner)
-    tile_body<true>(a, sm, X0, Z0, glm, gla, gmu, gb, gpart);
+    tile_body<true>(a, sm, X0, Z0, gpart);
   else
-    tile_body<false>(a, sm, X0, Z0, glm, gla, gmu, gb, gpart);
+    tile_body<false>(a, sm, X0, Z0, gpart);
 }
 
 }  // namespace
