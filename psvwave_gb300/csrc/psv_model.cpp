@@ -562,7 +562,7 @@ size_t Model::exact_lane_bytes(int C) const {
 }
 
 int Model::exact_lane_count(int C, int n_list) const {
-  // As many lanes as shots, at most kMaxLanes, within 60 % of the device
+  // As many lanes as shots, at most kMaxExactLanes, within 60 % of the device
   // memory that is free or already held by lanes.
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 1;
@@ -572,7 +572,7 @@ int Model::exact_lane_count(int C, int n_list) const {
   const size_t per = std::max<size_t>(exact_lane_bytes(C), 1);
   const size_t fit = static_cast<size_t>(0.6 * static_cast<double>(free_b)) / per;
   return static_cast<int>(std::max<size_t>(1, std::min<size_t>(
-      fit, static_cast<size_t>(std::min(n_list, kMaxLanes)))));
+      fit, static_cast<size_t>(std::min(n_list, kMaxExactLanes)))));
 }
 
 size_t Model::exact_bytes(int C) const {
@@ -972,6 +972,7 @@ double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
   // least two waves of resident CTAs between them; else the model's shape.
   // Measured at c3 (1100 x 500): eight lanes 1.07 s with 32 x 60 against
   // 1.14 s with 16 x 28; two lanes (every state kept) 0.88 s against 0.84 s.
+  // (Four lanes now: 4 x 315 tiles, still 32 x 60.)
   int ecfg = tile_cfg_;
   {
     const int big = tma::resident_ctas(tma::kTile32x60, false);

@@ -304,7 +304,9 @@ class Model {
   std::vector<std::unique_ptr<ExactLane>> lanes_;
   DeviceBuffer gff_shots_;
   cudaEvent_t lanes_start_ = nullptr;
-  static constexpr int kMaxLanes = 8;
+  static constexpr int kMaxLanes = 8;       // run_model lanes
+  static constexpr int kMaxExactLanes = 4;  // exact-gradient lanes (measured at c3: 4 lanes
+                                            // 1.02 s, 8 lanes 1.04 s, 2 lanes 1.15 s)
   static constexpr int kFlushSteps = 20;  // exact step: partial sums into the pairs
   int exact_lane_count(int C, int n_list) const;
   size_t exact_lane_bytes(int C) const;
