@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--ncu-case-exact", type=int, default=0, metavar="NT",
                    help="run one exact gradient of one NT-step shot of the c3 workload, launch by "
                         "launch, and exit (for ncu captures)")
+    p.add_argument("--ncu-case-cnn", type=int, default=0, metavar="B",
+                   help="run two surrogate-network predictions and one training step at B states "
+                        "and exit (for ncu captures)")
     return p.parse_args()
 
 
@@ -496,8 +499,30 @@ def ncu_case_exact(nt):
     print("ncu exact case: %s tiles, misfit %.9e" % (m.tile_shape, mis))
 
 
+def ncu_case_cnn(batch):
+    """Two predictions (four tensor-core convolutions and the head each) and
+    one Adam step of the c4 surrogate network at BATCH seeded random
+    states, for ncu captures."""
+    import torch
+    from psvwave_gb300 import surrogate as sg
+
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    net = sg.SurrogateNet(max_batch=batch, seed=1)
+    x = torch.randn(batch, 5, 20, 10, device="cuda", generator=gen)
+    m = torch.randn(batch, device="cuda", generator=gen)
+    g = torch.randn(batch, 3, 20, 10, device="cuda", generator=gen)
+    for _ in range(2):
+        mp, _ = net.predict_features(x)
+    net.train_step(x, m, g)
+    torch.cuda.synchronize()
+    print("ncu cnn case: %d states, misfit sum %.6e" % (batch, float(mp.sum())))
+
+
 def main():
     args = parse()
+    if args.ncu_case_cnn:
+        ncu_case_cnn(args.ncu_case_cnn)
+        return
     if args.ncu_case:
         ncu_case(args.ncu_case)
         return

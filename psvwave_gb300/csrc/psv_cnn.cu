@@ -33,60 +33,220 @@ __device__ __forceinline__ void tap(int k, int dil, int &dh, int &dc) {
   dc = (k % 3 - 1) * dil;
 }
 
-// y[b][co][p] = bias[co] + sum_ci sum_k w[co][ci][k] x[b][ci][p + off_k]
+// ---- tensor-core forward convolution (tcgen05) ---------------------------
+//
+// The forward convolution as an implicit GEMM on the 5th-generation tensor
+// cores: D[pos][co] = sum_k A[pos][k] W[co][k], with pos = b kP + p running
+// over the batch (kTcM = 128 positions per CTA, the MMA's M), co over the
+// output channels (N = cout rounded up to 16), and k = ci * 9 + tap over
+// the input channels and the 3 x 3 taps. K runs in chunks of kTcKc = 64:
+// seven input channels (63 columns) and one zero column, so that a column's
+// channel and tap are compile-time constants of the unrolled gather. Per
+// chunk each of the 128 threads gathers its position's row of the im2col
+// tile into shared memory (16-byte stores) as two BF16 matrices,
+// hi = bf16(x) and lo = bf16(x - hi), and the threads copy the chunk of
+// BF16 weights; one thread issues the tcgen05.mma instructions
+// (kind::f16, BF16 x BF16 -> FP32) for both, accumulating into a TMEM tile
+// of 128 lanes x 64 columns, and commits them to an mbarrier that every
+// thread waits on (bounded) before the next chunk overwrites the tiles.
+// Each warp then reads its 32 TMEM lanes (tcgen05.ld), adds the bias,
+// applies the ReLU and writes y[b][co][p].
+//
+// The hi + lo split carries the activations to about 2^-16 relative (the
+// products of BF16 values are exact in FP32), so the results match the FP32
+// FMA convolution to FP32-accumulation rounding: BF16 weights, FP32
+// activations and accumulation, as the network is specified.
+//
+// Shared-memory operands are K-major without swizzle: 8 x 16-byte core
+// matrices, element (r, k) at (r / 8) * kTcSBO + (k / 8) * 128 +
+// (r % 8) * 16 + (k % 8) * 2; the descriptor's leading byte offset (between
+// K-adjacent core matrices) is 128, its stride byte offset (between 8-row
+// groups) kTcSBO.
+constexpr int kTcM = 128, kTcKc = 64, kTcCi = 7, kTcThreads = 128, kTcCols = 64;
+constexpr int kTcLBO = 128, kTcSBO = (kTcKc / 8) * 128;
+
+__device__ __forceinline__ uint32_t tc_saddr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ int tc_off(int r, int k) {
+  return (r >> 3) * kTcSBO + (k >> 3) * kTcLBO + (r & 7) * 16 + (k & 7) * 2;
+}
+// Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading
+// byte offset >> 4 (16-29), stride byte offset >> 4 (32-45), descriptor
+// version 1 (bit 46), no swizzle (61-63 = 0).
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(kTcLBO >> 4) << 16) |
+         ((uint64_t)(kTcSBO >> 4) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
+  for (uint32_t i = 0; i < (1u << 20); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity), "r"(1000u)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 template <bool RELU>
-__global__ void __launch_bounds__(kThreads) conv_forward(int cin, int cout, int dil,
-                                                         const float *__restrict__ x,
-                                                         const __nv_bfloat16 *__restrict__ w,
-                                                         const float *__restrict__ bias,
-                                                         float *__restrict__ y) {
-  extern __shared__ float sm[];
-  float *xs = sm;                                                           // [cin][kP]
-  __nv_bfloat16 *ws = reinterpret_cast<__nv_bfloat16 *>(sm + kMaxC * kP);  // [kBlk][cin][9]
-  const int b = blockIdx.x, co0 = blockIdx.y * kBlk;
-  const int nco = min(kBlk, cout - co0);
-  const float *xb = x + (size_t)b * cin * kP;
-  for (int i = threadIdx.x; i < cin * kP; i += blockDim.x) xs[i] = xb[i];
-  for (int i = threadIdx.x; i < nco * cin * 9; i += blockDim.x) ws[i] = w[(size_t)co0 * cin * 9 + i];
-  __syncthreads();
-  const int p = threadIdx.x;
-  if (p >= kP) return;
-  const int h = p / kW, c = p - h * kW;
+__global__ void __launch_bounds__(kTcThreads) conv_forward_tc(int batch, int cin, int cout,
+                                                             int npad, int dil,
+                                                             const float *__restrict__ x,
+                                                             const __nv_bfloat16 *__restrict__ w,
+                                                             const float *__restrict__ bias,
+                                                             float *__restrict__ y, int *err) {
+  __shared__ __align__(1024) unsigned char a_hi[kTcM * kTcKc * 2];
+  __shared__ __align__(1024) unsigned char a_lo[kTcM * kTcKc * 2];
+  __shared__ __align__(1024) unsigned char b_w[kTcCols * kTcKc * 2];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_holder;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int total = batch * kP, pos0 = blockIdx.x * kTcM;
+  const int K = cin * 9;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc_saddr(&tmem_holder)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_saddr(&bar)), "r"(1)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // This thread's position for the gather (row tid of the tile) and the
+  // offsets of its nine taps within an input channel (-1 outside the image).
+  const int pos = pos0 + tid;
+  const bool row_ok = pos < total;
+  const int bs = row_ok ? pos / kP : 0, ps = row_ok ? pos - bs * kP : 0;
+  const int h = ps / kW, c = ps - h * kW;
   int nb[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) {
+  for (int t = 0; t < 9; ++t) {
     int dh, dc;
-    tap(k, dil, dh, dc);
+    tap(t, dil, dh, dc);
     const int hh = h + dh, cc = c + dc;
-    nb[k] = (hh >= 0 && hh < kH && cc >= 0 && cc < kW) ? hh * kW + cc : -1;
+    nb[t] = (row_ok && hh >= 0 && hh < kH && cc >= 0 && cc < kW) ? hh * kW + cc : -1;
   }
-  float acc[kBlk];
+  const float *xb = x + (size_t)bs * cin * kP;
+  // idesc: D FP32 (bits 4-5 = 1), A and B BF16 (7-9 = 1, 10-12 = 1), both
+  // K-major, N >> 3 (17-22), M >> 4 (24-28).
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(npad >> 3) << 17) |
+                         ((uint32_t)(kTcM >> 4) << 24);
+  bool ok = true;
+  uint32_t tmem = 0;
+  int ch = 0;
+  const int chunks = (cin + kTcCi - 1) / kTcCi;
+  for (; ch < chunks; ++ch) {
+    const int ci0 = ch * kTcCi;
 #pragma unroll
-  for (int o = 0; o < kBlk; ++o) acc[o] = 0.f;
-  for (int ci = 0; ci < cin; ++ci) {
-    const float *xr = xs + ci * kP;
-    float v[9];
+    for (int g = 0; g < kTcKc / 8; ++g) {
+      uint32_t hi2[4], lo2[4];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) v[k] = nb[k] >= 0 ? xr[nb[k]] : 0.f;
+      for (int e = 0; e < 8; e += 2) {
+        float v[2];
 #pragma unroll
-    for (int o = 0; o < kBlk; ++o) {
-      if (o < nco) {
-        const __nv_bfloat16 *wr = ws + (o * cin + ci) * 9;
-        float a = acc[o];
+        for (int q = 0; q < 2; ++q) {
+          const int kk = 8 * g + e + q, j = kk / 9, t = kk - 9 * (kk / 9);
+          v[q] = 0.f;
+          if (kk < 9 * kTcCi && ci0 + j < cin && nb[t] >= 0)
+            v[q] = __ldg(xb + (size_t)(ci0 + j) * kP + nb[t]);
+        }
+        const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[0], v[1]);
+        const float2 hf = __bfloat1622float2(h2);
+        const __nv_bfloat162 l2 = __floats2bfloat162_rn(v[0] - hf.x, v[1] - hf.y);
+        hi2[e / 2] = *reinterpret_cast<const uint32_t *>(&h2);
+        lo2[e / 2] = *reinterpret_cast<const uint32_t *>(&l2);
+      }
+      *reinterpret_cast<uint4 *>(a_hi + tc_off(tid, 8 * g)) =
+          make_uint4(hi2[0], hi2[1], hi2[2], hi2[3]);
+      *reinterpret_cast<uint4 *>(a_lo + tc_off(tid, 8 * g)) =
+          make_uint4(lo2[0], lo2[1], lo2[2], lo2[3]);
+    }
+    for (int i = tid; i < npad * kTcKc; i += kTcThreads) {
+      const int co = i / kTcKc, kk = i - co * kTcKc, k = ci0 * 9 + kk;
+      const __nv_bfloat16 v = (co < cout && kk < 9 * kTcCi && k < K)
+                                  ? w[(size_t)co * K + k]
+                                  : __float2bfloat16_rn(0.f);
+      *reinterpret_cast<__nv_bfloat16 *>(b_w + tc_off(co, kk)) = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem = tmem_holder;
+    if (tid == 0) {
+      for (int s = 0; s < kTcKc / 16; ++s) {
+        const uint32_t koff = s * 2 * kTcLBO;
+        const uint64_t bd = tc_desc(tc_saddr(b_w) + koff);
+        tc_mma(tmem, tc_desc(tc_saddr(a_hi) + koff), bd, idesc, (ch > 0 || s > 0) ? 1u : 0u);
+        tc_mma(tmem, tc_desc(tc_saddr(a_lo) + koff), bd, idesc, 1u);
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              tc_saddr(&bar))
+          : "memory");
+    }
+    // The chunk's products must be done before its tiles are overwritten.
+    if (!tc_wait(tc_saddr(&bar), (uint32_t)(ch & 1))) ok = false;
+    if (__syncthreads_or(!ok)) {
+      ok = false;
+      break;
+    }
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int row = 32 * warp + lane, g = pos0 + row;
+    const bool valid = g < total;
+    const int b = valid ? g / kP : 0, p = valid ? g - b * kP : 0;
+    for (int c0 = 0; c0 < npad; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+          "%14,%15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(ta));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (valid) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) a = fmaf(__bfloat162float(wr[k]), v[k], a);
-        acc[o] = a;
+        for (int j = 0; j < 16; ++j) {
+          const int co = c0 + j;
+          if (co < cout) {
+            float r = __uint_as_float(v[j]) + bias[co];
+            if (RELU) r = fmaxf(r, 0.f);
+            y[((size_t)b * cout + co) * kP + p] = r;
+          }
+        }
       }
     }
+  } else if (tid == 0) {
+    atomicOr(err, 1);
+    // Bounded: give the products of the chunk that timed out (the last ones
+    // issued) more time to finish before the TMEM is freed.
+    tc_wait(tc_saddr(&bar), (uint32_t)(ch & 1));
   }
-#pragma unroll
-  for (int o = 0; o < kBlk; ++o) {
-    if (o < nco) {
-      float r = acc[o] + bias[co0 + o];
-      if (RELU) r = fmaxf(r, 0.f);
-      y[((size_t)b * cout + co0 + o) * kP + p] = r;
-    }
-  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTcCols)
+                 : "memory");
 }
 
 // dx[b][ci][p] = (sum_co sum_k w[co][ci][k] dy[b][co][p - off_k]) * [act[b][ci][p] > 0]
@@ -306,10 +466,6 @@ void configure_once(int device) {
   const unsigned long long bit = 1ull << (device & 63);
   if (done & bit) return;
   const int smem = static_cast<int>(conv_smem());
-  check(cudaFuncSetAttribute(conv_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-        "conv smem");
-  check(cudaFuncSetAttribute(conv_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-        "conv smem");
   check(cudaFuncSetAttribute(conv_backward_data, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
         "conv smem");
   check(cudaFuncSetAttribute(conv_backward_weight, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -349,6 +505,20 @@ Net::Net(int device, int max_batch) : device_(device), max_batch_(max_batch) {
   for (auto &d : dact_) d.allocate((size_t)max_batch * kMaxC * kP * sizeof(float));
   loss_partials_.allocate((size_t)max_batch * sizeof(double));
   loss_.allocate(sizeof(double));
+  err_.allocate(sizeof(int));
+  check(cudaMemset(err_.get(), 0, sizeof(int)), "err flag");
+}
+
+// Raises when a tensor-core convolution's bounded wait for its products
+// timed out (the flag is cleared for the next call).
+void Net::check_error() {
+  int flag = 0;
+  check(cudaMemcpyAsync(&flag, err_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_), "err");
+  check(cudaStreamSynchronize(stream_), "err");
+  if (flag) {
+    check(cudaMemsetAsync(err_.get(), 0, sizeof(int), stream_), "err");
+    throw Error(PSV_ERR_CUDA, "a tensor-core convolution timed out waiting for its products");
+  }
 }
 
 Net::~Net() {
@@ -395,18 +565,18 @@ void Net::get_params(float *host) {
 
 void Net::forward(int batch, const float *x) {
   const float *in = x;
-  const size_t smem = conv_smem();
   for (int l = 0; l < kLayers; ++l) {
-    const dim3 grid(batch, (kCout[l] + kBlk - 1) / kBlk);
     const __nv_bfloat16 *w = wbf_.as<__nv_bfloat16>() + weight_offset(l);
     const float *bias = params_.as<float>() + bias_offset(l);
     float *out = act_[l].as<float>();
+    const int npad = std::max(16, (kCout[l] + 15) / 16 * 16);
+    const unsigned tiles = static_cast<unsigned>((batch * kP + kTcM - 1) / kTcM);
     if (l + 1 < kLayers)
-      conv_forward<true><<<grid, kThreads, smem, stream_>>>(kCin[l], kCout[l], kDil[l], in, w, bias,
-                                                           out);
+      conv_forward_tc<true><<<tiles, kTcThreads, 0, stream_>>>(
+          batch, kCin[l], kCout[l], npad, kDil[l], in, w, bias, out, err_.as<int>());
     else
-      conv_forward<false><<<grid, kThreads, smem, stream_>>>(kCin[l], kCout[l], kDil[l], in, w,
-                                                            bias, out);
+      conv_forward_tc<false><<<tiles, kTcThreads, 0, stream_>>>(
+          batch, kCin[l], kCout[l], npad, kDil[l], in, w, bias, out, err_.as<int>());
     check(cudaGetLastError(), "conv forward");
     in = out;
   }
@@ -441,6 +611,7 @@ double Net::backward(int batch, const float *x, const float *m_true, const float
   check(cudaMemcpyAsync(&loss, loss_.get(), sizeof(double), cudaMemcpyDeviceToHost, stream_),
         "loss");
   check(cudaStreamSynchronize(stream_), "backward");
+  check_error();
   return loss;
 }
 
@@ -451,6 +622,7 @@ void Net::predict(int batch, const float *x, float *misfit, float *grad) {
   head_predict<<<batch, kThreads, 0, stream_>>>(act_[kLayers - 1].as<float>(), misfit, grad);
   check(cudaGetLastError(), "head predict");
   check(cudaStreamSynchronize(stream_), "predict");
+  check_error();
 }
 
 double Net::loss_grad(int batch, const float *x, const float *m_true, const float *g_true,

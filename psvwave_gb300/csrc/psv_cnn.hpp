@@ -81,6 +81,8 @@ class Net {
   DeviceBuffer act_[kLayers];   // layer outputs [B][cout][kP] (post-ReLU for 1..3)
   DeviceBuffer dact_[2];        // gradient scratch [B][kMaxC][kP]
   DeviceBuffer loss_partials_, loss_;
+  DeviceBuffer err_;  // int, raised by a tensor-core convolution's bounded wait
+  void check_error();
 };
 
 }  // namespace cnn

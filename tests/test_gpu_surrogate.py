@@ -45,6 +45,20 @@ def test_forward_matches_oracle():
     assert rel_l2(g.cpu().numpy(), g_ref) <= 1e-4
 
 
+@pytest.mark.parametrize("B", [1, 300])
+def test_forward_tensor_core_tiles_match_oracle(B):
+    """The forward convolutions run as 128-position tensor-core tiles over
+    the whole batch: one image (a single partial tile) and a batch whose
+    last tile is ragged and whose tiles straddle images."""
+    net = sg.SurrogateNet(max_batch=512, seed=6)
+    params = net.get_params()
+    x, _, _ = rand_batch(B, 7)
+    m, g = net.predict_features(torch.tensor(x, device=DEV))
+    _, m_ref, g_ref = co.forward(params, x)
+    assert rel_l2(m.cpu().numpy(), m_ref) <= 1e-4
+    assert rel_l2(g.cpu().numpy(), g_ref) <= 1e-4
+
+
 def test_loss_gradient_matches_oracle():
     net = sg.SurrogateNet(max_batch=32, seed=4)
     params = net.get_params()
