@@ -267,10 +267,11 @@ def fwi_gradients_c3(steps, with_cpu=False):
     out["value"] = out["checkpoint_100"]["value"]
     # Algorithmic bytes of one checkpointed gradient: per shot and step two
     # forward steps (checkpoint pass, recompute; 52 B per cell each) and one
-    # exact step (107.2 B per cell: 18 words of fields and medium, FP32
-    # partial sums read and written, float-float pairs on one step in 20).
+    # exact step (98.4 B per cell: 18 words of fields and medium, three FP32
+    # partial sums read and written, three float-float pairs on one step in
+    # 20).
     cells = float(m.nx * m.nz)
-    per_grad = m.n_shots * m.nt * cells * (2 * 52.0 + 107.2)
+    per_grad = m.n_shots * m.nt * cells * (2 * 52.0 + 98.4)
     peak, kind = measured_peaks()
     t = out["checkpoint_100"]["ms_per_gradient"] / 1e3
     out["roofline"] = {"bound": "hbm", "bytes_per_gradient": per_grad,

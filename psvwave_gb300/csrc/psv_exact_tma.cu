@@ -29,11 +29,15 @@
 // lo: about 48 significant bits, like the FP64 sums of exact_step_tile, but
 // on the FP32 pipes (GB300 issues FP64 at a small fraction of the FP32
 // rate, and FP64 sums were most of this kernel's time). finish() turns the
-// pairs into FP64 once per gradient. With Step::g_part set, each step's
-// terms first go into an FP32 partial sum per point (one float4 for lm, la,
-// mu, b), which the flush steps (every few steps, and the last) add into
-// the pairs: per step the kernel then reads and writes 16 bytes of sums per
-// point instead of 32 (the pairs' traffic on flush steps only).
+// pairs into FP64 once per gradient. With Step::g_part_lmu set, each step's
+// terms first go into FP32 partial sums per point, which the flush steps
+// (every few steps, and the last) add into the pairs. There lambda's term
+// is folded into the gradients of lm and mu: the FP32 forward forms
+// lambda = lm - 2 mu, so d/dlm gains the lambda term and d/dmu loses twice
+// it, i.e. t_lm = dt (yxx + yzz)(exx + ezz) and t_mu = dt (yxz gxz -
+// 2 (yxx ezz + yzz exx)). Three sums (lm, mu | b) per point: per step the
+// kernel reads and writes 12 bytes of sums per point instead of 32 (and
+// the pairs of three gradients on flush steps only).
 //
 // Tiles whose 4-halo region lies inside the updated region and at least np
 // frames deep (taper exactly 1) and that hold no source point take a path
@@ -134,10 +138,11 @@ __device__ __forceinline__ float2 dxp_pair(float2 m1, float2 c0, float2 p1, floa
 // shared-memory access is a float2, and the z-direction stencils of the two
 // points share their loads. The difference coefficients are folded with
 // 1/dx and 1/dz. Phase 3: thread t owns points (X0 + t / 16,
-// Z0 + 2 (t % 16) + {0, 1}); gpart[q] are their partial sums.
+// Z0 + 2 (t % 16) + {0, 1}); plmu = (lm0, mu0, lm1, mu1) and pb = (b0, b1)
+// are their partial sums.
 template <bool INNER>
 __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int Z0,
-                                          const float4 *gpart) {
+                                          float4 plmu, float2 pb) {
   const int tid = threadIdx.x;
   const float c1 = 9.0f / 8.0f, c2 = 1.0f / 24.0f;
   const float c1x = c1 * a.idx, c2x = c2 * a.idx, c1z = c1 * a.idz, c2z = c2 * a.idz;
@@ -255,7 +260,7 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
   const int v = (lx + 4) * W + c;  // 4-halo boxes
   const float2 lxx = ld2(LXX + s), lzz = ld2(LZZ + s), lxz = ld2(LXZ + s);
   const float2 lvx = ld2(LVX + v), lvz = ld2(LVZ + v);
-  const bool part = a.g_part != nullptr;
+  const bool part = a.g_part_lmu != nullptr;
   const float lxxv[2] = {lxx.x, lxx.y}, lzzv[2] = {lzz.x, lzz.y}, lxzv[2] = {lxz.x, lxz.y};
   const float lvxv[2] = {lvx.x, lvx.y}, lvzv[2] = {lvz.x, lvz.y};
   // Per point: inside the grid, interior, taper.
@@ -327,6 +332,7 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
                                 c1x, c2x);
   const float exv[2] = {ex.x, ex.y}, ezv[2] = {ez.x, ez.y};
   const float gxzv[2] = {gxz_x.x + gxz_z.x, gxz_x.y + gxz_z.y};
+  float pl_lm[2] = {plmu.x, plmu.z}, pl_mu[2] = {plmu.y, plmu.w}, pl_b[2] = {pb.x, pb.y};
 #pragma unroll
   for (int e = 0; e < 2; ++e) {
     if (!validv[e]) continue;
@@ -337,23 +343,22 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
     float2 glm = make_float2(0.f, 0.f), gla = glm, gmu = glm, g_b = glm;
     if (!part || a.flush) {
       glm = a.g_lm[u];
-      gla = a.g_la[u];
+      if (!part) gla = a.g_la[u];
       gmu = a.g_mu[u];
       g_b = a.g_b[u];
     }
-    float4 gq = gpart[e];
-    float t_lm = 0.f, t_la = 0.f, t_mu = 0.f, t_b = 0.f;
+    float t_lm = 0.f, t_mu = 0.f, t_b = 0.f;
     if (inv[e]) {
       t_b = (a.dt * tp) * (lvxv[e] * axv[e] + lvzv[e] * azv[e]);
       const float yxx = tp * lxxv[e], yzz = tp * lzzv[e], yxz = tp * lxzv[e];
-      t_lm = a.dt * (yxx * exv[e] + yzz * ezv[e]);
-      t_la = a.dt * (yxx * ezv[e] + yzz * exv[e]);
-      t_mu = a.dt * yxz * gxzv[e];
       if (!part) {
         g_b = ff_add(g_b, t_b);
-        a.g_lm[u] = ff_add(glm, t_lm);
-        a.g_la[u] = ff_add(gla, t_la);
-        a.g_mu[u] = ff_add(gmu, t_mu);
+        a.g_lm[u] = ff_add(glm, a.dt * (yxx * exv[e] + yzz * ezv[e]));
+        a.g_la[u] = ff_add(gla, a.dt * (yxx * ezv[e] + yzz * exv[e]));
+        a.g_mu[u] = ff_add(gmu, a.dt * yxz * gxzv[e]);
+      } else {
+        t_lm = a.dt * ((yxx + yzz) * (exv[e] + ezv[e]));
+        t_mu = a.dt * (yxz * gxzv[e] - 2.f * (yxx * ezv[e] + yzz * exv[e]));
       }
     }
     // Source terms s = coef stf dt b / div at their points depend on b.
@@ -377,19 +382,23 @@ __device__ __forceinline__ void tile_body(const Step &a, float *sm, int X0, int 
       if (inv[e] || src) a.g_b[u] = g_b;
       continue;
     }
-    gq.x += t_lm;
-    gq.y += t_la;
-    gq.z += t_mu;
-    gq.w += t_b;
+    pl_lm[e] += t_lm;
+    pl_mu[e] += t_mu;
+    pl_b[e] += t_b;
     if (a.flush) {
-      a.g_lm[u] = ff_add(glm, gq.x);
-      a.g_la[u] = ff_add(gla, gq.y);
-      a.g_mu[u] = ff_add(gmu, gq.z);
-      a.g_b[u] = ff_add(g_b, gq.w);
-      a.g_part[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-    } else if (inv[e] || src) {
-      a.g_part[u] = gq;
+      a.g_lm[u] = ff_add(glm, pl_lm[e]);
+      a.g_mu[u] = ff_add(gmu, pl_mu[e]);
+      a.g_b[u] = ff_add(g_b, pl_b[e]);
+      pl_lm[e] = pl_mu[e] = pl_b[e] = 0.f;
     }
+  }
+  // The pair's partial sums (the second point may be row padding, where
+  // the sums stay 0).
+  if (part && validv[0]) {
+    const size_t q = (size_t)ix * a.pitch + iz;
+    reinterpret_cast<float4 *>(a.g_part_lmu + q)[0] =
+        make_float4(pl_lm[0], pl_mu[0], pl_lm[1], pl_mu[1]);
+    reinterpret_cast<float2 *>(a.g_part_b + q)[0] = make_float2(pl_b[0], pl_b[1]);
   }
 }
 
@@ -433,13 +442,15 @@ __global__ void __launch_bounds__(NT, 4)
   // (With partial sums, the pairs are read only on flush steps.)
   // (The float-float pairs are read in phase 3, where they are needed:
   // every step without partial sums, flush steps with them.)
-  float4 gpart[2];
+  // The pair's sums are adjacent in the padded rows (own_z is even and the
+  // pitch a multiple of 4), so they load as one float4 and one float2.
+  float4 plmu = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 pb = make_float2(0.f, 0.f);
   const int own_x = X0 + (tid >> 4), own_z = Z0 + 2 * (tid & 15);
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    const int ix = own_x, iz = own_z + j;
-    gpart[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (a.g_part && ix < a.nx && iz < a.nz) gpart[j] = a.g_part[(size_t)ix * a.nz + iz];
+  if (a.g_part_lmu && own_x < a.nx && own_z < a.nz) {
+    const size_t q = (size_t)own_x * a.pitch + own_z;
+    plmu = reinterpret_cast<const float4 *>(a.g_part_lmu + q)[0];
+    pb = reinterpret_cast<const float2 *>(a.g_part_b + q)[0];
   }
 
   const bool landed = mbar_wait(bar, 0, 1u << 20);
@@ -459,9 +470,9 @@ __global__ void __launch_bounds__(NT, 4)
                      !(pl.n && X0 < pl.x0 + pl.w && pl.x0 < X0 + TX && Z0 < pl.z0 + pl.h &&
                        pl.z0 < Z0 + TZ);
   if (inner)
-    tile_body<true>(a, sm, X0, Z0, gpart);
+    tile_body<true>(a, sm, X0, Z0, plmu, pb);
   else
-    tile_body<false>(a, sm, X0, Z0, gpart);
+    tile_body<false>(a, sm, X0, Z0, plmu, pb);
 }
 
 }  // namespace

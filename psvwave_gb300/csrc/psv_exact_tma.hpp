@@ -36,11 +36,16 @@ struct Step {
   float *olv[2] = {nullptr, nullptr};
   float *olt[3] = {nullptr, nullptr, nullptr};
   float2 *g_lm = nullptr, *g_la = nullptr, *g_mu = nullptr, *g_b = nullptr;
-  // Optional FP32 partial sums (lm, la, mu, b) per point of the unpadded
-  // grid: the step's terms are added there, and on a flush step the
-  // partial plus the terms go into the pairs and the partial is reset to 0.
-  // Null: every step adds into the pairs directly.
-  float4 *g_part = nullptr;
+  // Optional FP32 partial sums per point of the padded grid (index
+  // ix * pitch + iz): g_part_lmu holds (lm, mu), g_part_b holds b. The
+  // step's terms are added there, and on a flush step the partial plus the
+  // terms go into the pairs and the partial is reset to 0. With partial
+  // sums, lambda's term is folded into lm's and mu's (the FP32 forward
+  // forms lambda = lm - 2 mu, so these are the gradients of its inputs):
+  // g_la stays untouched. Null: every step adds the four terms into the
+  // pairs directly.
+  float2 *g_part_lmu = nullptr;
+  float *g_part_b = nullptr;
   int flush = 1;
   InjPlan plan{};
   const double *stf = nullptr;

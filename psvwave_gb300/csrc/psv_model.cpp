@@ -558,7 +558,8 @@ size_t Model::exact_lane_bytes(int C) const {
   const size_t state = 5 * padded_size() * elem();
   const size_t n_ck = (nt + C - 1) / C;
   return n_ck * state + (C + 1) * state + kLamPlanes * padded_size() * elem() +
-         2 * static_cast<size_t>(cfg_.nr) * nt * sizeof(float) + grid_size() * sizeof(float4);
+         2 * static_cast<size_t>(cfg_.nr) * nt * sizeof(float) +
+         padded_size() * (sizeof(float2) + sizeof(float));
 }
 
 int Model::exact_lane_count(int C, int n_list) const {
@@ -997,7 +998,7 @@ double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
     ensure(l->slots, (C + 1) * state_bytes);
     ensure(l->lam, kLamPlanes * field_bytes);
     ensure(l->raw, std::max<size_t>(2 * static_cast<size_t>(nr) * nt * sizeof(float), 16));
-    ensure(l->part, g * sizeof(float4));
+    ensure(l->part, gp * (sizeof(float2) + sizeof(float)));
   }
   for (auto &b : gex_) ensure(b, g * sizeof(double));
   for (auto &b : kexact_) ensure(b, g * sizeof(double));
@@ -1037,7 +1038,8 @@ double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
     unsigned char *ck = l.ckpt.as<unsigned char>(), *sl = l.slots.as<unsigned char>();
     float2 *gs = gff_shots_.as<float2>() + static_cast<size_t>(shot) * 4 * g;
     cuda_check(cudaMemsetAsync(gs, 0, 4 * g * sizeof(float2), s), "exact zero");
-    cuda_check(cudaMemsetAsync(l.part.get(), 0, g * sizeof(float4), s), "exact zero");
+    cuda_check(cudaMemsetAsync(l.part.get(), 0, gp * (sizeof(float2) + sizeof(float)), s),
+               "exact zero");
     auto state = [&](unsigned char *base, void *out[5]) {
       for (int f = 0; f < 5; ++f) out[f] = base + f * field_bytes;
     };
@@ -1134,9 +1136,11 @@ double Model::exact_gradient_lanes(int C, const std::vector<int> &shot_list) {
         x.g_la = gs + g;
         x.g_mu = gs + 2 * g;
         x.g_b = gs + 3 * g;
-        // Terms go into FP32 partial sums, added into the float-float pairs
-        // every kFlushSteps steps and at step 0.
-        x.g_part = l.part.as<float4>();
+        // Terms go into FP32 partial sums (lambda's folded into lm's and
+        // mu's), added into the float-float pairs every kFlushSteps steps
+        // and at step 0.
+        x.g_part_lmu = l.part.as<float2>();
+        x.g_part_b = reinterpret_cast<float *>(l.part.as<unsigned char>() + gp * sizeof(float2));
         x.flush = (n % kFlushSteps == 0) ? 1 : 0;
         x.plan = plans_[shot];
         x.stf = stf_d_.as<double>();

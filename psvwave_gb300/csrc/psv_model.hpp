@@ -284,7 +284,8 @@ class Model {
   struct ExactLane {
     cudaStream_t stream = nullptr;  // own stream (lanes >= 1)
     cudaEvent_t done = nullptr;
-    DeviceBuffer ckpt, slots, lam, raw, part;  // part: FP32 partial gradient sums
+    // part: FP32 partial gradient sums, (lm, mu) pairs then b, padded grid
+    DeviceBuffer ckpt, slots, lam, raw, part;
     std::vector<tma::Maps> slot_maps;  // input maps of each state slot
     exact_tma::Maps emaps;             // the exact step's maps over lam, slots, medium
     const void *maps_slots = nullptr;  // slots / lam / C / tile shape the maps were made for
