@@ -332,6 +332,13 @@ int psv_batch_info(const psv_batch *b, int *members, int *tiles, double *cells);
  * flags[k] != 0; NULL = all (the default). Inactive members' CTAs exit at
  * once, so the captured time loop serves every subset. */
 int psv_batch_set_active(psv_batch *b, const int *flags, int n);
+/* L2 misfit of each member's model after psv_batch_forward, as
+ * psv_calculate_l2_misfit computes it (src/fdModel.cpp:1128-1145), bit for
+ * bit: out[k] for the n == members members in the order added (NaN for
+ * inactive ones), one reduction per member on the batch's stream and one
+ * copy back. Each active model's misfit is updated as
+ * psv_calculate_l2_misfit would. */
+int psv_batch_misfits(psv_batch *b, double *out, int n);
 /* Launch scheme of psv_batch_forward: 0 (the default) launches once per
  * time step, the loop captured as one CUDA graph; persistent != 0 runs every
  * time step of every member in one persistent launch over the batch's tile
@@ -339,6 +346,16 @@ int psv_batch_set_active(psv_batch *b, const int *flags, int n);
  * previous one. Results are identical. */
 int psv_batch_set_persistent(psv_batch *b, int persistent);
 int psv_batch_get_persistent(const psv_batch *b, int *persistent);
+/* Cluster-resident scheme: cluster != 0 runs every member in its own
+ * thread-block cluster that keeps the member's whole grid in shared memory
+ * for every time step, all members in one launch (the batched form of the
+ * model variant fused_cluster, whose results it equals bit for bit).
+ * PSV_ERR_INVALID_ARGUMENT when a member does not fit a cluster; *fits
+ * (psv_batch_cluster_fits) tells beforehand. psv_batch_set_persistent
+ * switches it off; psv_batch_autotune also times it when the members fit. */
+int psv_batch_set_cluster(psv_batch *b, int cluster);
+int psv_batch_get_cluster(const psv_batch *b, int *cluster);
+int psv_batch_cluster_fits(psv_batch *b, int *fits);
 
 /* ---- no-allocation entry point ------------------------------------------ */
 /* L2 misfit 0.5 dt sum((obs - syn)^2) over both components, written to the

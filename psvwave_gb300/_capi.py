@@ -133,6 +133,10 @@ _SIGNATURES = {
     "psv_batch_autotune": [_vp, _c_int, _ip],
     "psv_batch_info": [_vp, _ip, _ip, _dp],
     "psv_batch_set_active": [_vp, _ip, _c_int],
+    "psv_batch_misfits": [_vp, _dp, _c_int],
+    "psv_batch_set_cluster": [_vp, _c_int],
+    "psv_batch_get_cluster": [_vp, _ip],
+    "psv_batch_cluster_fits": [_vp, _ip],
     "psv_batch_get_persistent": [_vp, ctypes.POINTER(ctypes.c_int)],
     "psv_batch_set_persistent": [_vp, _c_int],
     "psv_l2_misfit_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_size_t, _c_double, _vp, _vp],

@@ -51,6 +51,27 @@ class Batch:
         Results are identical."""
         _capi.check(self._lib.psv_batch_set_persistent(self._h, int(bool(on))))
 
+    @property
+    def cluster(self):
+        v = ctypes.c_int()
+        _capi.check(self._lib.psv_batch_get_cluster(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
+    @cluster.setter
+    def cluster(self, on):
+        """Cluster-resident scheme (True): every member in its own
+        thread-block cluster holding its whole grid in shared memory for
+        every step, all members in one launch; results equal each model's
+        own `fused_cluster` run bit for bit. ValueError when a member does
+        not fit (`cluster_fits`). Setting `persistent` switches it off."""
+        _capi.check(self._lib.psv_batch_set_cluster(self._h, int(bool(on))))
+
+    @property
+    def cluster_fits(self):
+        v = ctypes.c_int()
+        _capi.check(self._lib.psv_batch_cluster_fits(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
     def set_active(self, mask=None):
         """Members the next forward() advances (a boolean per member, in the
         order added); None = all."""
@@ -65,6 +86,17 @@ class Batch:
     def forward(self, store_fields=False, n_steps=0):
         _capi.check(self._lib.psv_batch_forward(self._h, int(bool(store_fields)), int(n_steps)))
 
+    def misfits(self):
+        """L2 misfit of each member's model after forward() (float64, one per
+        member in the order added; NaN for inactive members), equal bit for
+        bit to each model's calculate_l2_misfit(), which it also updates:
+        one reduction per member and one copy back."""
+        import numpy as np
+        out = np.empty(len(self._models), dtype=np.float64)
+        _capi.check(self._lib.psv_batch_misfits(
+            self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.size))
+        return out
+
     @property
     def tile_shape(self):
         return self._tile_shape if hasattr(self, "_tile_shape") else "16x28"
@@ -75,9 +107,10 @@ class Batch:
         self._tile_shape = name
 
     def autotune(self, n_steps=50):
-        """Times every tile shape with both launch schemes on n_steps steps
-        of the active members and keeps the fastest pair; returns the shape
-        (the scheme is `persistent`)."""
+        """Times every tile shape with both tile launch schemes, and the
+        cluster-resident scheme when the members fit, on n_steps steps of
+        the active members and keeps the fastest; returns the tile shape
+        (the scheme is `cluster`, else `persistent`)."""
         v = ctypes.c_int()
         _capi.check(self._lib.psv_batch_autotune(self._h, int(n_steps), ctypes.byref(v)))
         self._tile_shape = {0: "32x60", 1: "16x28", 2: "20x28", 3: "16x60"}[v.value]

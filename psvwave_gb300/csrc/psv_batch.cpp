@@ -2,8 +2,10 @@
 #include "psv_batch.hpp"
 
 #include <algorithm>
+#include <limits>
 
 #include "../../include/psvwave.h"
+#include "psv_cluster.hpp"
 
 namespace psv {
 
@@ -52,6 +54,34 @@ void Batch::add(Model *m, int shot) {
   members_.emplace_back(m, shot);
   active_h_.push_back(1);
   built_ = false;
+  cluster_nc_ = -1;
+  cluster_ = false;
+  clear_graphs();
+}
+
+bool Batch::cluster_fits() {
+  if (cluster_nc_ < 0) {
+    std::vector<int> nx, nz, np;
+    for (const auto &mb : members_) {
+      nx.push_back(mb.first->geometry().nx);
+      nz.push_back(mb.first->geometry().nz);
+      np.push_back(mb.first->config().np_boundary);
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    cluster_nc_ = cluster::plan_batch(nx.data(), nz.data(), np.data(), static_cast<int>(nx.size()),
+                                      &cluster_smem_);
+    cudaSetDevice(prev);
+  }
+  return cluster_nc_ > 0;
+}
+
+void Batch::set_cluster(bool on) {
+  if (on && !cluster_fits())
+    throw Error(PSV_ERR_INVALID_ARGUMENT, "a batch member does not fit a thread-block cluster");
+  if (on == cluster_) return;
+  cluster_ = on;
   clear_graphs();
 }
 
@@ -176,8 +206,9 @@ void Batch::set_tile_cfg(int cfg) {
 }
 
 void Batch::set_persistent(bool on) {
-  if (on == persistent_) return;
+  if (on == persistent_ && !cluster_) return;
   persistent_ = on;
+  cluster_ = false;
   clear_graphs();
 }
 
@@ -220,7 +251,11 @@ void Batch::forward(bool store, int n_steps) {
   const int cfg = tile_cfg_;
   auto enqueue = [&]() {
     cuda_check(cudaMemsetAsync(arena_.get(), 0, arena_.bytes(), stream_), "batch zero");
-    if (persistent_) {
+    if (cluster_) {
+      cuda_check(cluster::steps_batch(descs_d_.as<tma::SimDesc>(), active_.as<int>(), size(),
+                                      cluster_nc_, cluster_smem_, steps, store, stream_),
+                 "batch cluster steps");
+    } else if (persistent_) {
       cuda_check(cudaMemsetAsync(sched_.get(), 0, sched_.bytes(), stream_), "batch schedule");
       cuda_check(tma::steps_persistent_batch(descs_d_.as<tma::SimDesc>(),
                                              tiles_d_[cfg].as<int4>(), n_tiles_[cfg],
@@ -285,11 +320,54 @@ void Batch::forward(bool store, int n_steps) {
   }
 }
 
+void Batch::misfits(double *out, int n) {
+  if (n != size()) throw Error(PSV_ERR_INVALID_ARGUMENT, "expected one value per member");
+  if (members_.empty()) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+  struct Restore {
+    int dev;
+    ~Restore() { cudaSetDevice(dev); }
+  } restore{prev};
+  if (misfit_d_.bytes() < static_cast<size_t>(n) * sizeof(double))
+    misfit_d_.allocate(static_cast<size_t>(n) * sizeof(double));
+  auto active = [&](int k) {
+    return k >= static_cast<int>(active_h_.size()) || active_h_[k] != 0;
+  };
+  for (int k = 0; k < n; ++k) {
+    if (!active(k)) continue;
+    Model &m = *members_[k].first;
+    // The same reduction as Model::calculate_l2_misfit, into slot k.
+    const size_t nd = m.data_size();
+    int parts = static_cast<int>(std::min<size_t>(Model::kPartials, (nd + 255) / 256));
+    if (parts < 1) parts = 1;
+    cuda_check(misfit_l2(nd, m.cfg_.dt, m.rtf_true_[0].as<double>(), m.rtf_[0].as<double>(),
+                         m.rtf_true_[1].as<double>(), m.rtf_[1].as<double>(),
+                         m.partials_.as<double>(), parts, misfit_d_.as<double>() + k, stream_),
+               "batch misfits");
+  }
+  std::vector<double> v(n);
+  cuda_check(cudaMemcpyAsync(v.data(), misfit_d_.get(), static_cast<size_t>(n) * sizeof(double),
+                             cudaMemcpyDeviceToHost, stream_),
+             "batch misfits copy");
+  synchronize();
+  for (int k = 0; k < n; ++k) {
+    if (active(k)) {
+      out[k] = v[k];
+      members_[k].first->misfit_ = v[k];
+    } else {
+      out[k] = std::numeric_limits<double>::quiet_NaN();
+    }
+  }
+}
+
 int Batch::autotune(int n_steps) {
   if (members_.empty()) return tile_cfg_;
   // Every (launch scheme, tile shape) pair on n_steps steps of the members
   // currently active, each timed on its third run (after the build and the
-  // graph capture); the fastest pair is kept.
+  // graph capture), and the cluster-resident scheme when the members fit;
+  // the fastest is kept.
   float best = 0;
   int best_cfg = tile_cfg_;
   bool best_persistent = persistent_, first = true;
@@ -316,10 +394,24 @@ int Batch::autotune(int n_steps) {
       }
     }
   }
+  bool best_cluster = false;
+  if (cluster_fits()) {
+    set_cluster(true);
+    forward(false, n_steps);
+    forward(false, n_steps);
+    cudaEventRecord(a, stream_);
+    forward(false, n_steps);
+    cudaEventRecord(b, stream_);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) best_cluster = true;
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   set_persistent(best_persistent);
   set_tile_cfg(best_cfg);
+  if (best_cluster) set_cluster(true);
   return best_cfg;
 }
 

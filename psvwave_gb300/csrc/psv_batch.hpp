@@ -35,12 +35,26 @@ class Batch {
   // Which members the next forward() advances (non-zero = advance); all of
   // them by default. The others keep their previous seismograms.
   void set_active(const int *flags, int n);
+  // L2 misfit of every active member's model (what calculate_l2_misfit
+  // returns, bit for bit; n == size()), one reduction per member on the
+  // batch's stream and one copy back; inactive members get NaN. Each active
+  // model's misfit is updated as calculate_l2_misfit would.
+  void misfits(double *out, int n);
   // Launch scheme: one launch per time step (false, the default) or every
   // step in one persistent launch over the tile table (true). A batch step
   // holds tens of thousands of tiles, many waves with no tail to recover,
   // so the per-item scheduling of the persistent scheme is measured slower.
   void set_persistent(bool on);
   bool persistent() const { return persistent_; }
+  // Cluster-resident scheme: every member in its own thread-block cluster
+  // that holds its whole grid in shared memory for every step, all members
+  // in one launch (members must fit: cluster_fits()). Takes precedence over
+  // the tile schemes while on; set_persistent() switches it off. Results
+  // equal each model's own cluster-resident run (variant fused_cluster) bit
+  // for bit.
+  bool cluster_fits();
+  void set_cluster(bool on);
+  bool cluster() const { return cluster_; }
   int tile_cfg() const { return tile_cfg_; }
   int size() const { return static_cast<int>(members_.size()); }
   double cells() const;  // grid points summed over members
@@ -64,8 +78,12 @@ class Batch {
   int n_tiles_[tma::kNumTileCfgs] = {};
   DeviceBuffer err_flag_;
   DeviceBuffer active_;              // per member flag, read by the step kernel
+  DeviceBuffer misfit_d_;            // per member misfit (misfits())
   std::vector<int> active_h_;
   bool persistent_ = false;
+  bool cluster_ = false;
+  int cluster_nc_ = -1;      // -1: not planned yet; 0: the members do not fit
+  size_t cluster_smem_ = 0;
   DeviceBuffer sched_;               // persistent scheme: item counter, tile progress
   DeviceBuffer rec_start_, rec_list_;  // receivers by member tile (persistent scheme)
   std::vector<size_t> raw_off_;  // per member, floats into raw_

@@ -671,10 +671,41 @@ int psv_batch_get_persistent(const psv_batch *b, int *persistent) {
   });
 }
 
+int psv_batch_set_cluster(psv_batch *b, int cluster) {
+  return guarded([&] {
+    need(b, "batch");
+    b->impl.set_cluster(cluster != 0);
+  });
+}
+
+int psv_batch_get_cluster(const psv_batch *b, int *cluster) {
+  return guarded([&] {
+    need(b, "batch");
+    need(cluster, "cluster");
+    *cluster = b->impl.cluster() ? 1 : 0;
+  });
+}
+
+int psv_batch_cluster_fits(psv_batch *b, int *fits) {
+  return guarded([&] {
+    need(b, "batch");
+    need(fits, "fits");
+    *fits = b->impl.cluster_fits() ? 1 : 0;
+  });
+}
+
 int psv_batch_set_active(psv_batch *b, const int *flags, int n) {
   return guarded([&] {
     need(b, "batch");
     b->impl.set_active(flags, n);
+  });
+}
+
+int psv_batch_misfits(psv_batch *b, double *out, int n) {
+  return guarded([&] {
+    need(b, "batch");
+    need(out, "out");
+    b->impl.misfits(out, n);
   });
 }
 

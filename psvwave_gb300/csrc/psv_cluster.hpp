@@ -32,5 +32,18 @@ int plan(int nx, int nz, int np);
 cudaError_t steps(const tma::SimDesc &d, bool adjoint, int it0, int n_steps, int parity,
                   bool store, int nc, cudaStream_t s);
 
+// Batched forward: the cluster size for members of sizes nx[k] x nz[k]
+// (np[k] frames), k < n, each in its own cluster (the largest member's
+// shared memory per CTA, returned in *smem), or 0 when one does not fit.
+// Sets the batch kernel's launch attributes (call outside stream capture).
+int plan_batch(const int *nx, const int *nz, const int *np, int n, size_t *smem);
+
+// Forward steps 0 .. n_steps - 1 of the n simulations of the device table
+// `sims`, from set 0 (final state in set n_steps & 1), one cluster of nc
+// CTAs each, in one launch; with `active` non-null only members flagged
+// non-zero run.
+cudaError_t steps_batch(const tma::SimDesc *sims, const int *active, int n, int nc, size_t smem,
+                        int n_steps, bool store, cudaStream_t s);
+
 }  // namespace cluster
 }  // namespace psv

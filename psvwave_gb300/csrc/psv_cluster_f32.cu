@@ -51,10 +51,11 @@ size_t smem_bytes(int R, int S, int np) {
   return ((size_t)(5 * (R + 4) + 3 * R) * S + (size_t)(np + 1)) * sizeof(float);
 }
 
+// The time loop of one simulation in the calling cluster (every CTA of the
+// cluster calls it with the same arguments).
 template <bool ADJ>
-__global__ void __launch_bounds__(NT, 1)
-    cluster_steps(const __grid_constant__ tma::SimDesc d, int nc, int it0, int n_steps,
-                  int parity, int store) {
+__device__ __forceinline__ void member_steps(const tma::SimDesc &d, int nc, int it0, int n_steps,
+                                             int parity, int store) {
   cg::cluster_group cl = cg::this_cluster();
   const int k = (int)cl.block_rank();
   const int nx = d.nx, nz = d.nz, ps = d.pitch, np = d.np;
@@ -228,6 +229,25 @@ __global__ void __launch_bounds__(NT, 1)
 }
 
 template <bool ADJ>
+__global__ void __launch_bounds__(NT, 1)
+    cluster_steps(const __grid_constant__ tma::SimDesc d, int nc, int it0, int n_steps,
+                  int parity, int store) {
+  member_steps<ADJ>(d, nc, it0, n_steps, parity, store);
+}
+
+// Forward steps 0 .. n_steps - 1 of a batch: cluster m (CTAs m nc ..
+// m nc + nc - 1) runs simulation sims[m] from set 0; a cluster whose flag in
+// `active` is zero returns at once (the whole cluster: no barrier is left
+// waiting). Two CTAs per SM, so that twice as many clusters run at once.
+__global__ void __launch_bounds__(NT, 2)
+    cluster_steps_batch(const tma::SimDesc *__restrict__ sims, const int *__restrict__ active,
+                        int nc, int n_steps, int store) {
+  const int m = (int)(blockIdx.x / (unsigned)nc);
+  if (active && !active[m]) return;
+  member_steps<false>(sims[m], nc, 0, n_steps, 0, store);
+}
+
+template <bool ADJ>
 bool configure(size_t smem, int nc) {
   if (cudaFuncSetAttribute(cluster_steps<ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
@@ -256,7 +276,76 @@ bool placeable(size_t smem, int nc) {
   return cudaOccupancyMaxActiveClusters(&n, cluster_steps<ADJ>, &lc) == cudaSuccess && n >= 1;
 }
 
+bool configure_batch(size_t smem, int nc) {
+  if (cudaFuncSetAttribute(cluster_steps_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return false;
+  if (nc > 8 &&
+      cudaFuncSetAttribute(cluster_steps_batch, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                           1) != cudaSuccess)
+    return false;
+  return true;
+}
+
+bool placeable_batch(size_t smem, int nc) {
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = nc;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.gridDim = dim3(nc);
+  lc.blockDim = dim3(NT);
+  lc.dynamicSmemBytes = smem;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  int n = 0;
+  return cudaOccupancyMaxActiveClusters(&n, cluster_steps_batch, &lc) == cudaSuccess && n >= 1;
+}
+
 }  // namespace
+
+int plan_batch(const int *nx, const int *nz, const int *np, int n, size_t *smem_out) {
+  int dev = 0, optin = 0;
+  if (n <= 0 || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+          cudaSuccess)
+    return 0;
+  for (int nc : {16, 8}) {
+    size_t smem = 0;
+    bool fits = true;
+    for (int k = 0; k < n && fits; ++k) {
+      if (nx[k] < 2 * nc) fits = false;
+      smem = std::max(smem, smem_bytes(max_rows(nc, nx[k]), stride(nz[k]), np[k]));
+    }
+    if (!fits || smem > (size_t)optin) continue;
+    if (!configure_batch((size_t)optin, nc)) continue;
+    if (placeable_batch(smem, nc)) {
+      if (smem_out) *smem_out = smem;
+      return nc;
+    }
+  }
+  cudaGetLastError();  // a refused non-portable size is not an error here
+  return 0;
+}
+
+cudaError_t steps_batch(const tma::SimDesc *sims, const int *active, int n, int nc, size_t smem,
+                        int n_steps, bool store, cudaStream_t s) {
+  if (n_steps <= 0 || n <= 0) return cudaSuccess;
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = nc;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.gridDim = dim3((unsigned)(n * nc));
+  lc.blockDim = dim3(NT);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = s;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, cluster_steps_batch, sims, active, nc, n_steps, store ? 1 : 0);
+}
 
 int plan(int nx, int nz, int np) {
   int dev = 0, optin = 0;

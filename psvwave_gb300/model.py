@@ -509,7 +509,7 @@ class fdModel:
     # Device buffers (torch CUDA tensors, float64, contiguous). Inputs are read
     # on this model's stream after the caller's current stream has finished
     # with them; outputs are complete when the call returns.
-    def _device_tensor(self, t, shape, name):
+    def _device_tensor(self, t, shape, name, sync=True):
         import torch
 
         if tuple(t.shape) != tuple(shape):
@@ -517,7 +517,8 @@ class fdModel:
         if not t.is_cuda or t.device.index != self.device:
             raise ValueError("tensor %s must live on cuda:%d" % (name, self.device))
         t = t.detach().to(torch.float64).contiguous()
-        torch.cuda.current_stream(t.device).synchronize()
+        if sync:
+            torch.cuda.current_stream(t.device).synchronize()
         return t
 
     def _device_out(self, shape):
@@ -525,10 +526,15 @@ class fdModel:
 
         return torch.empty(shape, dtype=torch.float64, device="cuda:%d" % self.device)
 
-    def set_parameter_fields_device(self, vp, vs, rho):
-        """set_parameter_fields from CUDA tensors [nx, nz]."""
+    def set_parameter_fields_device(self, vp, vs, rho, sync=True):
+        """set_parameter_fields from CUDA tensors [nx, nz]. sync=False skips
+        the wait for torch's current stream: the caller has already waited
+        for the tensors (float64, contiguous) and keeps them alive until the
+        model's stream has copied them (with set_async(True) the copies and
+        the medium update are only queued on the model's stream)."""
         shape = (self.nx, self.nz)
-        t = [self._device_tensor(a, shape, n) for a, n in zip((vp, vs, rho), ("_vp", "_vs", "_rho"))]
+        t = [self._device_tensor(a, shape, n, sync)
+             for a, n in zip((vp, vs, rho), ("_vp", "_vs", "_rho"))]
         _capi.check(self._lib.psv_set_parameter_fields_device(
             self._h, *[ctypes.cast(x.data_ptr(), _DP) for x in t]))
 

@@ -227,6 +227,9 @@ class FDPosterior:
         for _ in range(n_models):
             m = fdModel.from_parameters(params, device=device)
             m.set_observed_data(*observed)
+            # Media updates are only queued on the model's stream; the batched
+            # forward and the exact gradient wait for it.
+            m.set_async(True)
             self.models.append(m)
         self.batch = Batch(device)
         for m in self.models:
@@ -237,8 +240,8 @@ class FDPosterior:
         self.n_potentials = 0
         self.n_gradients = 0
 
-    def _set(self, k, fields_k):
-        self.models[k].set_parameter_fields_device(fields_k[0], fields_k[1], fields_k[2])
+    def _set(self, k, fields_k, sync=True):
+        self.models[k].set_parameter_fields_device(fields_k[0], fields_k[1], fields_k[2], sync)
 
     def misfits(self, z, mask=None):
         """FD misfits of z [B][3][20][10] (B <= n_models), one batched
@@ -251,16 +254,19 @@ class FDPosterior:
         out = np.full(B, np.nan)
         if not sel.any():
             return out
+        # One wait for the fields; each model then only queues its copies
+        # and medium update (the batched forward waits for every member's
+        # stream, and `fields` lives until it returns).
         fields = self.coarse.to_fields(z)
+        torch.cuda.current_stream(fields.device).synchronize()
         for k in np.flatnonzero(sel):
-            self._set(k, fields[k])
+            self._set(k, fields[k], sync=False)
         flags = np.zeros(len(self.models), dtype=bool)
         flags[:B] = sel
         self.batch.set_active(flags)
         self.batch.forward()
-        for k in np.flatnonzero(sel):
-            self.models[k].calculate_l2_misfit()
-            out[k] = self.models[k].misfit
+        mis = self.batch.misfits()
+        out[sel] = mis[:B][sel]
         self.n_potentials += int(sel.sum())
         return out
 

@@ -95,3 +95,90 @@ def test_batch_subset_matches_full_run(persistent):
             assert np.array_equal(ux[0], full[k][0][0]) and np.array_equal(uz[0], full[k][1][0])
         else:
             assert not ux[0].any() and not uz[0].any()
+
+
+def test_batch_misfits_equal_each_models_misfit():
+    # One reduction per active member, bit for bit what each model's own
+    # calculate_l2_misfit gives; NaN for members switched off.
+    models = small_models()
+    for m in models:
+        m.set_observed_data(*[0.5 * a for a in m.get_synthetic_data()])
+    b = psv.Batch()
+    for m in models:
+        b.add(m, 0)
+    mask = [True, False, True]
+    b.set_active(mask)
+    b.forward()
+    mis = b.misfits()
+    assert mis.shape == (len(models),)
+    for k, m in enumerate(models):
+        if mask[k]:
+            assert mis[k] == m.misfit  # the model's misfit is updated
+            m.calculate_l2_misfit()
+            assert mis[k] == m.misfit and mis[k] > 0
+        else:
+            assert np.isnan(mis[k])
+
+
+def cluster_models(nt=300):
+    # c0-size members and a smaller one: every member fits a cluster.
+    models = []
+    for k, (nxi, nzi) in enumerate([(200, 100), (200, 100), (120, 64)]):
+        p = dict(workloads.c0_params(), nt=nt, nx_inner=nxi, nz_inner=nzi)
+        p["ix_sources"] = [nxi // 3, 2 * nxi // 3]
+        p["iz_sources"] = [nzi // 2, nzi // 2]
+        p["ix_receivers"] = [5 + 5 * j for j in range(19)]
+        m = psv.fdModel.from_parameters(p)
+        nx, nz = m.nx, m.nz
+        rng = np.random.default_rng(10 + k)
+        vp = 2000.0 * (1 + 0.05 * rng.standard_normal((nx, nz)))
+        m.set_parameter_fields(vp, 0.4 * vp, np.full((nx, nz), 1500.0))
+        models.append(m)
+    return models
+
+
+def test_batch_cluster_scheme_matches_model_cluster_runs():
+    # Every member in its own cluster, all in one launch: each model's own
+    # cluster-resident run (variant fused_cluster) bit for bit, for the
+    # members switched on; the others keep their seismograms.
+    models = cluster_models()
+    ref = []
+    for m in models:
+        m.kernel_variant = "fused_cluster"
+        m.forward_simulate(0, False)
+        ref.append([a.copy() for a in m.get_synthetic_data()])
+        m.set_synthetic_data(*[np.zeros_like(a) for a in m.get_synthetic_data()])
+    b = psv.Batch()
+    for m in models:
+        b.add(m, 0)
+    assert b.cluster_fits
+    b.cluster = True
+    assert b.cluster
+    for _ in range(3):  # eager, graph capture, graph replay
+        b.forward()
+        for m, out in zip(models, ref):
+            ux, uz = m.get_synthetic_data()
+            assert np.array_equal(ux, out[0]) and np.array_equal(uz, out[1])
+    for m in models:
+        m.set_synthetic_data(*[np.zeros_like(a) for a in m.get_synthetic_data()])
+    mask = [True, False, True]
+    b.set_active(mask)
+    b.forward()
+    for k, m in enumerate(models):
+        ux, uz = m.get_synthetic_data()
+        if mask[k]:
+            assert np.array_equal(ux, ref[k][0]) and np.array_equal(uz, ref[k][1])
+        else:
+            assert not ux.any() and not uz.any()
+    b.persistent = False  # switches the cluster scheme off
+    assert not b.cluster
+
+
+def test_batch_cluster_scheme_refused_for_large_members():
+    models = small_models(2)  # c2-size members, too large for a cluster
+    b = psv.Batch()
+    for m in models:
+        b.add(m, 0)
+    if not b.cluster_fits:
+        with pytest.raises(ValueError):
+            b.cluster = True
