@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--ncu-case-exact", type=int, default=0, metavar="NT",
                    help="run one exact gradient of one NT-step shot of the c3 workload, launch by "
                         "launch, and exit (for ncu captures)")
+    p.add_argument("--ncu-case-c4judge", type=int, default=0, metavar="SHAPE",
+                   help="run one batched forward of the c4 judge (128 members) with the tile "
+                        "shape given by index (0 32x60, 1 16x28, 2 20x28, 3 16x60; one launch "
+                        "per step) and exit (for ncu captures)")
     p.add_argument("--ncu-case-cnn", type=int, default=0, metavar="B",
                    help="run two surrogate-network predictions and one training step at B states "
                         "and exit (for ncu captures)")
@@ -500,6 +504,24 @@ def ncu_case_exact(nt):
     print("ncu exact case: %s tiles, misfit %.9e" % (m.tile_shape, mis))
 
 
+def ncu_case_c4judge(shape):
+    """One batched forward (2000 steps) of the c4 posterior's judge over its
+    128 members at seeded prior states, with tile shape index SHAPE and one
+    launch per step, for ncu captures (set-up and tuning launches come
+    first)."""
+    import torch
+    from psvwave_gb300 import surrogate as sg
+
+    S = sg.c4_setup(128, s2=1.0)
+    post = S["posterior"]
+    post.batch.persistent = False
+    post.batch.tile_shape = {0: "32x60", 1: "16x28", 2: "20x28", 3: "16x60"}[shape]
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    z = 0.5 * torch.randn((128, 3, 20, 10), device="cuda", generator=gen)
+    mis = post.misfits(z)
+    print("ncu c4 judge case: %s tiles, misfit sum %.9e" % (post.batch.tile_shape, mis.sum()))
+
+
 def ncu_case_cnn(batch):
     """Two predictions (four tensor-core convolutions and the head each) and
     one Adam step of the c4 surrogate network at BATCH seeded random
@@ -523,6 +545,9 @@ def main():
     args = parse()
     if args.ncu_case_cnn:
         ncu_case_cnn(args.ncu_case_cnn)
+        return
+    if args.ncu_case_c4judge:
+        ncu_case_c4judge(args.ncu_case_c4judge)
         return
     if args.ncu_case:
         ncu_case(args.ncu_case)

@@ -138,12 +138,24 @@ __device__ __forceinline__ float col_taper(const SimDesc &d, int gz) {
   return tz < d.np ? __ldg(d.taper_tab + tz) : 1.0f;
 }
 
-// Phases B and C of an interior tile (TAPER false: taper exactly 1) or a
-// taper tile (TAPER true). Phase B: each thread walks SR / G consecutive
-// rows of one column, keeping the x-direction stencil values of vx and vz in
-// registers (one new shared load each per row); phase C: KC consecutive
-// rows per thread with the x-direction windows of txx and txz.
-template <class S, bool ADJ, bool TAPER, class Mid = NoHook>
+// Frame-count taper of a row or column at grid index g of an n-point axis,
+// for any g (points outside the grid clamp to the table's first entry; their
+// updates are masked out).
+__device__ __forceinline__ float axis_taper(const SimDesc &d, int g, int n) {
+  const int t = max(min(g + 1, n - g), 0);
+  return t < d.np ? __ldg(d.taper_tab + t) : 1.0f;
+}
+
+// Phases B and C of an interior tile (TAPER false: taper exactly 1), a
+// taper tile (TAPER true) or a frame tile of a one-column shape (FRAME true:
+// the box may reach past the grid's edges; per-point taper min(column
+// factor, row factor) and masks that keep points outside the updated region
+// 2 <= x < n-2 at their old values, and own points past the grid unwritten).
+// Phase B: each thread walks SR / G consecutive rows of one column, keeping
+// the x-direction stencil values of vx and vz in registers (one new shared
+// load each per row); phase C: KC consecutive rows per thread with the
+// x-direction windows of txx and txz.
+template <class S, bool ADJ, bool TAPER, bool FRAME = false, class Mid = NoHook>
 __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields &out, int X0,
                                             int Z0, const float (*VX)[S::W],
                                             const float (*VZ)[S::W], float (*sxx_)[S::W],
@@ -165,7 +177,9 @@ __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields
     const int gz = Z0 - 4 + c;
     const bool z_own = c >= 4 && c < TZ + 4;
     const int r0 = q * RB;
-    const float tzc = TAPER ? col_taper(d, gz) : 1.0f;
+    const float tzc = FRAME ? axis_taper(d, gz, d.nz) : TAPER ? col_taper(d, gz) : 1.0f;
+    const bool zi = !FRAME || (gz >= 2 && gz < d.nz - 2);
+    const bool z_out = !FRAME || gz < d.nz;
     float xm1 = VX[r0 + 1][c], x0 = VX[r0 + 2][c], xp1 = VX[r0 + 3][c], xp2 = VX[r0 + 4][c];
     float zm2 = VZ[r0][c], zm1 = VZ[r0 + 1][c], z0 = VZ[r0 + 2][c], zp1 = VZ[r0 + 3][c];
     int gp = (X0 - 2 + r0) * ps + gz;
@@ -180,7 +194,15 @@ __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields
                         (c1 * (z0 - zm1) + c2 * (zm2 - zp1)) * idx;
       const float ex = dvx * idx, ez = dvz * idz;
       float sxx, szz, sxz;
-      if (TAPER) {
+      if (FRAME) {
+        const int gx = X0 - 2 + r;
+        const float tp = fminf(tzc, axis_taper(d, gx, d.nx));
+        const bool u = zi && gx >= 2 && gx < d.nx - 2;
+        const float oxx = sxx_[r][c], ozz = szz_[r][c], oxz = sxz_[r][c];
+        sxx = u ? tp * (oxx + dtv * (lm * ex + la * ez)) : oxx;
+        szz = u ? tp * (ozz + dtv * (la * ex + lm * ez)) : ozz;
+        sxz = u ? tp * (oxz + dtv * mu * gxz) : oxz;
+      } else if (TAPER) {
         const float tp = fminf(tzc, row_taper(d, X0 - 2 + r));
         sxx = tp * (sxx_[r][c] + dtv * (lm * ex + la * ez));
         szz = tp * (szz_[r][c] + dtv * (la * ex + lm * ez));
@@ -193,7 +215,7 @@ __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields
       sxx_[r][c] = sxx;
       szz_[r][c] = szz;
       sxz_[r][c] = sxz;
-      if (z_own && r >= 2 && r < TX + 2) {
+      if (z_own && r >= 2 && r < TX + 2 && z_out && (!FRAME || X0 - 2 + r < d.nx)) {
         out.txx[gp] = sxx;
         out.tzz[gp] = szz;
         out.txz[gp] = sxz;
@@ -220,7 +242,9 @@ __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields
     const int cc = lzc + 4;
     const int lx0 = q * KC;
     const int s0 = lx0 + 2;  // stress box row of the first point
-    const float tzc = TAPER ? col_taper(d, gzc) : 1.0f;
+    const float tzc = FRAME ? axis_taper(d, gzc, d.nz) : TAPER ? col_taper(d, gzc) : 1.0f;
+    const bool zi = !FRAME || (gzc >= 2 && gzc < d.nz - 2);
+    const bool z_out = !FRAME || gzc < d.nz;
     float am2 = TXX[s0 - 2][cc], am1 = TXX[s0 - 1][cc], a0 = TXX[s0][cc], ap1 = TXX[s0 + 1][cc];
     float bm1 = TXZ[s0 - 1][cc], b0 = TXZ[s0][cc], bp1 = TXZ[s0 + 1][cc], bp2 = TXZ[s0 + 2][cc];
     int gq = (X0 + lx0) * ps + gzc;
@@ -232,7 +256,16 @@ __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields
       const float az = (c1 * (bp1 - b0) + c2 * (bm1 - bp2)) * idx +
                        (c1 * (TZZ[r][cc + 1] - TZZ[r][cc]) + c2 * (TZZ[r][cc - 1] - TZZ[r][cc + 2])) * idz;
       const float bdt = bb[k] * dtv;
-      if (TAPER) {
+      if (FRAME) {
+        const int gx = X0 + lx;
+        const float tp = fminf(tzc, axis_taper(d, gx, d.nx));
+        const bool u = zi && gx >= 2 && gx < d.nx - 2;
+        const float ovx = VX[lx + 4][cc], ovz = VZ[lx + 4][cc];
+        if (z_out && gx < d.nx) {
+          out.vx[gq] = u ? tp * (ovx + bdt * ax) : ovx;
+          out.vz[gq] = u ? tp * (ovz + bdt * az) : ovz;
+        }
+      } else if (TAPER) {
         const float tp = fminf(tzc, row_taper(d, X0 + lx));
         out.vx[gq] = tp * (VX[lx + 4][cc] + bdt * ax);
         out.vz[gq] = tp * (VZ[lx + 4][cc] + bdt * az);
@@ -253,14 +286,6 @@ __device__ __forceinline__ void tile_phases(const SimDesc &d, const fast::Fields
       }
     }
   }
-}
-
-// Frame-count taper of a row or column at grid index g of an n-point axis,
-// for any g (points outside the grid clamp to the table's first entry; their
-// updates are masked out).
-__device__ __forceinline__ float axis_taper(const SimDesc &d, int g, int n) {
-  const int t = max(min(g + 1, n - g), 0);
-  return t < d.np ? __ldg(d.taper_tab + t) : 1.0f;
 }
 
 // A frame tile has no snapshot I/O this step, no injection term, and its own
@@ -524,6 +549,10 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   constexpr bool V2 = S::TZ == 60;
   const bool frame = V2 && !inner && frame_tile<S>(d, X0, Z0, snap_io);
   const bool tapered = TAPERED && !inner && taper_tile<S>(d, X0, Z0, snap_io);
+  // One-column shapes: the other tiles without snapshot I/O or injection
+  // take the register-window path with masks (frame tiles).
+  const bool frame1 = TAPERED && !V2 && !inner && !tapered && !snap_io &&
+                      !injection_tile<S>(d, X0, Z0);
 
   // This thread's buoyancy values for phase C (the medium does not change
   // between steps, so they load before the previous step has finished).
@@ -551,7 +580,7 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   } else {
 #pragma unroll
     for (int k = 0; k < KC; ++k) {
-      const int gx = (inner || tapered) ? X0 + q * KC + k : X0 + q + G * k;
+      const int gx = (inner || tapered || frame1) ? X0 + q * KC + k : X0 + q + G * k;
       bb[k] = (col_ok && gx < nx) ? __ldg(d.b + gx * ps + gzc) : 0.f;
     }
   }
@@ -633,6 +662,10 @@ __device__ __forceinline__ bool step_body(const SimDesc &d, const Maps &maps, in
   }
   if (TAPERED && tapered) {
     tile_phases<S, ADJ, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb, mid);
+    return true;
+  }
+  if (TAPERED && frame1) {
+    tile_phases<S, ADJ, true, true>(d, out, X0, Z0, VX, VZ, sxx_, szz_, sxz_, slm, smu, bb, mid);
     return true;
   }
 
@@ -944,9 +977,21 @@ cudaError_t launch(const SimDesc *sims, const int4 *tiles, int n_tiles, const in
   cudaError_t e = configure(fused_step_tma_batch<S, CFG, ADJ>, S::SMEM, configured);
   if (e != cudaSuccess) return e;
   if (n_tiles <= 0) return cudaSuccess;
-  fused_step_tma_batch<S, CFG, ADJ><<<n_tiles, S::NT, S::SMEM, s>>>(sims, tiles, active, it,
-                                                                    parity, store, err);
-  return cudaGetLastError();
+  // Programmatic stream serialisation, as for the single-model step: the
+  // CTAs of this step may become resident while the previous step's last
+  // wave drains; they wait in griddep_wait before touching any wave field.
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(n_tiles);
+  lc.blockDim = dim3(S::NT);
+  lc.dynamicSmemBytes = S::SMEM;
+  lc.stream = s;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, fused_step_tma_batch<S, CFG, ADJ>, sims, tiles, active, it,
+                            parity, store, err);
 }
 
 template <class S, int CFG, bool ADJ>
