@@ -1,13 +1,15 @@
 // Surrogate network kernels (forward, backward, Adam) and the coarse-to-grid
 // parameter map of the Monte Carlo workload; see psv_cnn.hpp.
 //
-// Convolutions run one CTA per (sample, block of 8 output channels): the
-// sample's input channels [cin][20 x 10] are staged in shared memory with the
-// block's BF16 weights, and each of 200 threads computes one output pixel of
-// the 8 channels with FP32 FMAs. The backward pass mirrors it: input
-// gradients per (sample, block of 8 input channels), with the next layer's
-// ReLU mask fused in; weight gradients per (output channel, batch chunk) as
-// fixed-order partial sums that a second kernel adds up.
+// The forward convolutions and the weight gradients run on the tensor cores
+// (tcgen05 implicit GEMMs with BF16 hi + lo operand splits and FP32
+// accumulators in TMEM; see conv_forward_tc and conv_weight_tc). Input
+// gradients run one CTA per (sample, block of 8 input channels): the
+// sample's output gradients [cout][20 x 10] are staged in shared memory with
+// the block's BF16 weights, each of 200 threads computes one pixel with FP32
+// FMAs, and the next layer's ReLU mask is fused in. Weight gradients are
+// fixed-order partial sums over position ranges that a second kernel adds
+// up, so every result is deterministic.
 #include "psv_cnn.hpp"
 
 #include <algorithm>
@@ -249,6 +251,168 @@ __global__ void __launch_bounds__(kTcThreads) conv_forward_tc(int batch, int cin
                  : "memory");
 }
 
+// ---- tensor-core weight gradients (tcgen05) --------------------------------
+//
+// dW[co][k] = sum_pos dy[pos][co] X[pos][k] and db[co] = sum_pos dy[pos][co]
+// as a GEMM whose reduction runs over the positions pos = b kP + p of the
+// batch: D[k][co] (M = 128 rows of k = ci * 9 + tap per CTA, the bias as row
+// k = cin * 9 with X = 1; N = cout rounded up to 16) accumulates
+// A[k][pos] B[co][pos] over chunks of 64 positions, with A = X^T the
+// transposed im2col of the layer input and B = dy^T. Both operands are FP32
+// values split into BF16 hi + lo parts; hi.hi + hi.lo + lo.hi (three
+// tcgen05.mma kind::f16 per 16 positions) carry the products to about 2^-16
+// relative, the FP32 accumulation order is fixed, and blockIdx.y splits the
+// chunks into kChunks ranges whose partial sums sum_chunks adds in order
+// (deterministic). Per chunk thread t gathers position t % 64 of rows
+// (t / 64) * 64 .. + 63 of A and every other row of B, one thread issues
+// the MMAs and commits them to an mbarrier every thread waits on (bounded;
+// a time-out raises the error flag). The epilogue reads row 32 w + lane of
+// the accumulator (tcgen05.ld.32x32b) and writes the CTA's partial sums in
+// the layout of the weights ((co cin + ci) 9 + tap, then the biases).
+__global__ void __launch_bounds__(kTcThreads) conv_weight_tc(int batch, int cin, int cout,
+                                                            int npad, int dil,
+                                                            const float *__restrict__ x,
+                                                            const float *__restrict__ dy,
+                                                            float *__restrict__ partial, int *err) {
+  __shared__ __align__(1024) unsigned char a_hi[kTcM * kTcKc * 2];
+  __shared__ __align__(1024) unsigned char a_lo[kTcM * kTcKc * 2];
+  __shared__ __align__(1024) unsigned char b_hi[kTcCols * kTcKc * 2];
+  __shared__ __align__(1024) unsigned char b_lo[kTcCols * kTcKc * 2];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_holder;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int K = cin * 9;  // weight columns; row K is the bias
+  const int m0 = blockIdx.x * kTcM;
+  const int total = batch * kP;
+  const int n_chunks = (total + kTcKc - 1) / kTcKc;
+  const int c0 = (int)((long long)n_chunks * blockIdx.y / gridDim.y);
+  const int c1 = (int)((long long)n_chunks * (blockIdx.y + 1) / gridDim.y);
+  const size_t len = (size_t)cout * K + cout;
+  float *out = partial + (size_t)blockIdx.y * len;
+  const int k_out = m0 + 32 * warp + lane;  // the accumulator row this thread writes
+  auto out_index = [&](int co) {
+    return k_out < K ? (size_t)co * K + k_out : (size_t)cout * K + co;
+  };
+  if (c0 >= c1) {  // no positions in this range: zero partial sums
+    if (k_out <= K)
+      for (int co = 0; co < cout; ++co) out[out_index(co)] = 0.f;
+    return;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc_saddr(&tmem_holder)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_saddr(&bar)), "r"(1)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(npad >> 3) << 17) |
+                         ((uint32_t)(kTcM >> 4) << 24);
+  const int j = tid & 63, half = tid >> 6;
+  bool ok = true;
+  uint32_t tmem = 0;
+  int ch = c0;
+  for (; ch < c1; ++ch) {
+    const int g = ch * kTcKc + j;
+    const bool valid = g < total;
+    const int b = valid ? g / kP : 0, p = valid ? g - b * kP : 0;
+    const int h = p / kW, c = p - h * kW;
+    const float *xb = x + (size_t)b * cin * kP;
+    // A: rows half * 64 .. + 63 at position column j.
+    int k = m0 + half * 64;
+    int ci = k / 9, t = k - 9 * ci;
+    for (int mm = 0; mm < 64; ++mm, ++k) {
+      float v = 0.f;
+      if (k < K) {
+        int dh, dc;
+        tap(t, dil, dh, dc);
+        const int hh = h + dh, cc = c + dc;
+        if (valid && hh >= 0 && hh < kH && cc >= 0 && cc < kW)
+          v = __ldg(xb + (size_t)ci * kP + hh * kW + cc);
+      } else if (k == K) {
+        v = valid ? 1.f : 0.f;
+      }
+      const __nv_bfloat16 vh = __float2bfloat16_rn(v);
+      const __nv_bfloat16 vl = __float2bfloat16_rn(v - __bfloat162float(vh));
+      *reinterpret_cast<__nv_bfloat16 *>(a_hi + tc_off(half * 64 + mm, j)) = vh;
+      *reinterpret_cast<__nv_bfloat16 *>(a_lo + tc_off(half * 64 + mm, j)) = vl;
+      if (++t == 9) {
+        t = 0;
+        ++ci;
+      }
+    }
+    // B: rows co = half, half + 2, ... at position column j.
+    for (int co = half; co < npad; co += 2) {
+      const float v =
+          (valid && co < cout) ? __ldg(dy + ((size_t)b * cout + co) * kP + p) : 0.f;
+      const __nv_bfloat16 vh = __float2bfloat16_rn(v);
+      const __nv_bfloat16 vl = __float2bfloat16_rn(v - __bfloat162float(vh));
+      *reinterpret_cast<__nv_bfloat16 *>(b_hi + tc_off(co, j)) = vh;
+      *reinterpret_cast<__nv_bfloat16 *>(b_lo + tc_off(co, j)) = vl;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem = tmem_holder;
+    if (tid == 0) {
+      for (int s = 0; s < kTcKc / 16; ++s) {
+        const uint32_t koff = s * 2 * kTcLBO;
+        const uint64_t ah = tc_desc(tc_saddr(a_hi) + koff), al = tc_desc(tc_saddr(a_lo) + koff);
+        const uint64_t bh = tc_desc(tc_saddr(b_hi) + koff), bl = tc_desc(tc_saddr(b_lo) + koff);
+        tc_mma(tmem, ah, bh, idesc, (ch > c0 || s > 0) ? 1u : 0u);
+        tc_mma(tmem, ah, bl, idesc, 1u);
+        tc_mma(tmem, al, bh, idesc, 1u);
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              tc_saddr(&bar))
+          : "memory");
+    }
+    // The chunk's products must be done before its tiles are overwritten.
+    if (!tc_wait(tc_saddr(&bar), (uint32_t)((ch - c0) & 1))) ok = false;
+    if (__syncthreads_or(!ok)) {
+      ok = false;
+      break;
+    }
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    for (int col = 0; col < npad; col += 16) {
+      uint32_t v[16];
+      const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)col;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+          "%14,%15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(ta));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (k_out <= K) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+          if (col + q < cout) out[out_index(col + q)] = __uint_as_float(v[q]);
+      }
+    }
+  } else if (tid == 0) {
+    atomicOr(err, 1);
+    // Bounded: give the products of the chunk that timed out more time to
+    // finish before the TMEM is freed.
+    tc_wait(tc_saddr(&bar), (uint32_t)((ch - c0) & 1));
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTcCols)
+                 : "memory");
+}
+
 // dx[b][ci][p] = (sum_co sum_k w[co][ci][k] dy[b][co][p - off_k]) * [act[b][ci][p] > 0]
 __global__ void __launch_bounds__(kThreads) conv_backward_data(int cin, int cout, int dil,
                                                                const float *__restrict__ dy,
@@ -303,64 +467,6 @@ __global__ void __launch_bounds__(kThreads) conv_backward_data(int cin, int cout
       const size_t i = ((size_t)b * cin + ci0 + o) * kP + p;
       dx[i] = act[i] > 0.f ? acc[o] : 0.f;
     }
-  }
-}
-
-// Partial weight and bias gradients of output channel blockIdx.x over the
-// samples of batch chunk blockIdx.y: partial[chunk][(co*cin+ci)*9+k] and
-// partial[chunk][cout*cin*9 + co].
-__global__ void __launch_bounds__(kThreads) conv_backward_weight(int batch, int cin, int cout,
-                                                                 int dil,
-                                                                 const float *__restrict__ x,
-                                                                 const float *__restrict__ dy,
-                                                                 float *__restrict__ partial) {
-  extern __shared__ float sm[];
-  float *xs = sm;                // [cin][kP]
-  float *ds = sm + kMaxC * kP;   // [kP]
-  const int co = blockIdx.x, chunk = blockIdx.y;
-  const int b0 = (int)((long long)batch * chunk / kChunks);
-  const int b1 = (int)((long long)batch * (chunk + 1) / kChunks);
-  const int nslot = cin * 9 + 1;  // the last slot is the bias
-  constexpr int kSlots = (kMaxC * 9 + 1 + kThreads - 1) / kThreads;
-  float acc[kSlots];
-#pragma unroll
-  for (int j = 0; j < kSlots; ++j) acc[j] = 0.f;
-  for (int b = b0; b < b1; ++b) {
-    const float *xb = x + (size_t)b * cin * kP;
-    for (int i = threadIdx.x; i < cin * kP; i += blockDim.x) xs[i] = xb[i];
-    for (int i = threadIdx.x; i < kP; i += blockDim.x) ds[i] = dy[((size_t)b * cout + co) * kP + i];
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < kSlots; ++j) {
-      const int s = threadIdx.x + j * kThreads;
-      if (s >= nslot) continue;
-      float a = acc[j];
-      if (s == nslot - 1) {
-        for (int p = 0; p < kP; ++p) a += ds[p];
-      } else {
-        const int ci = s / 9, k = s - ci * 9;
-        int dh, dc;
-        tap(k, dil, dh, dc);
-        const float *xr = xs + ci * kP;
-        const int h0 = max(0, -dh), h1 = min(kH, kH - dh);
-        const int c0 = max(0, -dc), c1 = min(kW, kW - dc);
-        for (int h = h0; h < h1; ++h)
-          for (int c = c0; c < c1; ++c) a = fmaf(ds[h * kW + c], xr[(h + dh) * kW + c + dc], a);
-      }
-      acc[j] = a;
-    }
-    __syncthreads();
-  }
-  const size_t len = (size_t)cout * cin * 9 + cout;
-  float *out = partial + (size_t)chunk * len;
-#pragma unroll
-  for (int j = 0; j < kSlots; ++j) {
-    const int s = threadIdx.x + j * kThreads;
-    if (s >= nslot) continue;
-    if (s == nslot - 1)
-      out[(size_t)cout * cin * 9 + co] = acc[j];
-    else
-      out[(size_t)co * cin * 9 + s] = acc[j];
   }
 }
 
@@ -467,9 +573,6 @@ void configure_once(int device) {
   if (done & bit) return;
   const int smem = static_cast<int>(conv_smem());
   check(cudaFuncSetAttribute(conv_backward_data, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-        "conv smem");
-  check(cudaFuncSetAttribute(conv_backward_weight, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem),
         "conv smem");
   done |= bit;
 }
@@ -592,8 +695,11 @@ double Net::backward(int batch, const float *x, const float *m_true, const float
   check(cudaGetLastError(), "head loss");
   for (int l = kLayers - 1; l >= 0; --l) {
     const float *in = l == 0 ? x : act_[l - 1].as<float>();
-    conv_backward_weight<<<dim3(kCout[l], kChunks), kThreads, smem, stream_>>>(
-        batch, kCin[l], kCout[l], kDil[l], in, cur, partials_.as<float>());
+    const int rows = kCin[l] * 9 + 1;  // weights of one output channel, then its bias
+    const unsigned mtiles = static_cast<unsigned>((rows + kTcM - 1) / kTcM);
+    conv_weight_tc<<<dim3(mtiles, kChunks), kTcThreads, 0, stream_>>>(
+        batch, kCin[l], kCout[l], std::max(16, (kCout[l] + 15) / 16 * 16), kDil[l], in, cur,
+        partials_.as<float>(), err_.as<int>());
     const size_t len = layer_size(l);
     sum_chunks<<<blocks(len), 256, 0, stream_>>>(len, partials_.as<float>(),
                                                  grads_.as<float>() + weight_offset(l));

@@ -35,7 +35,7 @@ constexpr int kCin[kLayers] = {5, 32, 64, 64};
 constexpr int kCout[kLayers] = {32, 64, 64, 4};
 constexpr int kDil[kLayers] = {1, 2, 4, 1};
 constexpr int kMaxC = 64;
-constexpr int kChunks = 8;  // batch chunks of the weight-gradient partial sums
+constexpr int kChunks = 32;  // position ranges of the weight-gradient partial sums
 
 // Parameter vector layout: for each layer, weights [cout][cin][3][3] then
 // bias [cout].

@@ -73,6 +73,36 @@ def test_loss_gradient_matches_oracle():
         assert rel_l2(d[a:b], d_ref[a:b]) <= 1e-4, l
 
 
+def test_loss_gradient_matches_oracle_ragged_batch():
+    """The weight gradients reduce positions in 64-position chunks over 32
+    ranges on the tensor cores: a batch whose positions end inside a chunk
+    and whose ranges straddle images. At this size some pre-activations of
+    a random network lie within the forward's FP32 rounding of the ReLU
+    kink, where the GPU's mask and the FP64 oracle's may differ. A large
+    first-layer bias and non-negative weights and positive biases in the
+    next two layers keep every hidden pre-activation well away from it, so
+    the comparison checks the arithmetic, not the kink."""
+    net = sg.SurrogateNet(max_batch=256, seed=8)
+    params = net.get_params()
+    offs, _ = co.offsets()
+    for l in range(3):
+        nw = co.COUT[l] * co.CIN[l] * 9
+        if l > 0:
+            params[offs[l]:offs[l] + nw] = np.abs(params[offs[l]:offs[l] + nw])
+        params[offs[l] + nw:offs[l] + nw + co.COUT[l]] = 8.0 if l == 0 else 1.0
+    net.set_params(params)
+    params = net.get_params()
+    x, m, g = rand_batch(130, 9)
+    acts, _, _ = co.forward(params, x)
+    assert min(float(a.min()) for a in acts[:3]) > 0.1  # no ReLU kink nearby
+    loss, d = net.loss_grad(*to_dev(x, m, g), w_misfit=1.0, w_grad=1.0)
+    loss_ref, d_ref = co.loss_grad(params, x, m, g, 1.0, 1.0)
+    assert abs(loss - loss_ref) <= 1e-5 * abs(loss_ref)
+    for l in range(4):
+        a, b = offs[l], offs[l] + co.layer_size(l)
+        assert rel_l2(d[a:b], d_ref[a:b]) <= 1e-4, l
+
+
 def test_adam_step_matches_oracle():
     net = sg.SurrogateNet(max_batch=8, seed=5)
     p0 = net.get_params().astype(np.float64)
