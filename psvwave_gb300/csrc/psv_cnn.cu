@@ -54,10 +54,11 @@ __device__ __forceinline__ void tap(int k, int dil, int &dh, int &dc) {
 // Each warp then reads its 32 TMEM lanes (tcgen05.ld), adds the bias,
 // applies the ReLU and writes y[b][co][p].
 //
-// The hi + lo split carries the activations to about 2^-16 relative (the
-// products of BF16 values are exact in FP32), so the results match the FP32
-// FMA convolution to FP32-accumulation rounding: BF16 weights, FP32
-// activations and accumulation, as the network is specified.
+// The hi + lo split keeps 16 significant bits of each activation (about
+// 2^-17 relative; the products of BF16 values are exact in FP32), so the
+// results are the FP32 convolution of the activations so rounded, up to
+// accumulation order: BF16 weights, FP32 activations and accumulation, as
+// the network is specified, to about 1e-6 relative.
 //
 // Shared-memory operands are K-major without swizzle: 8 x 16-byte core
 // matrices, element (r, k) at (r / 8) * kTcSBO + (k / 8) * 128 +
