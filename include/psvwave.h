@@ -339,6 +339,15 @@ int psv_batch_set_active(psv_batch *b, const int *flags, int n);
  * copy back. Each active model's misfit is updated as
  * psv_calculate_l2_misfit would. */
 int psv_batch_misfits(psv_batch *b, double *out, int n);
+/* psv_set_parameter_fields_device (src/psvWave.cpp:256-297, from device
+ * arrays) for every member k with flags[k] != 0 (all when flags is NULL):
+ * its vp, vs and rho ([nx][nz] each, consecutive) start at
+ * fields + k * member_stride (doubles, device memory). A model that is a
+ * member more than once is set once; each model queues its copies and
+ * medium update on its own stream, as its own call does, and the next
+ * psv_batch_forward waits for them. */
+int psv_batch_set_parameter_fields_device(psv_batch *b, const double *fields,
+                                          long long member_stride, const int *flags);
 /* Launch scheme of psv_batch_forward: 0 (the default) launches once per
  * time step, the loop captured as one CUDA graph; persistent != 0 runs every
  * time step of every member in one persistent launch over the batch's tile

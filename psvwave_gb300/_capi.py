@@ -134,6 +134,7 @@ _SIGNATURES = {
     "psv_batch_info": [_vp, _ip, _ip, _dp],
     "psv_batch_set_active": [_vp, _ip, _c_int],
     "psv_batch_misfits": [_vp, _dp, _c_int],
+    "psv_batch_set_parameter_fields_device": [_vp, _vp, ctypes.c_longlong, _ip],
     "psv_batch_set_cluster": [_vp, _c_int],
     "psv_batch_get_cluster": [_vp, _ip],
     "psv_batch_cluster_fits": [_vp, _ip],

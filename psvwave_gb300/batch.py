@@ -86,6 +86,37 @@ class Batch:
     def forward(self, store_fields=False, n_steps=0):
         _capi.check(self._lib.psv_batch_forward(self._h, int(bool(store_fields)), int(n_steps)))
 
+    def set_parameter_fields_device(self, fields, mask=None):
+        """set_parameter_fields for many members at once: `fields` is a CUDA
+        float64 tensor whose row k holds member k's (vp, vs, rho), each
+        [nx][nz] (rows past the last flagged member are not read); `mask`
+        selects the members (all by default). One wait for torch's stream,
+        then each model queues its copies and medium update on its own
+        stream; forward() waits for them. Keep `fields` alive until then."""
+        import numpy as np
+        import torch
+        if not fields.is_cuda or fields.dtype != torch.float64 or not fields.is_contiguous():
+            raise ValueError("fields must be a contiguous float64 CUDA tensor")
+        n = len(self._models)
+        if mask is None:
+            flags = np.ones(n, dtype=np.int32)
+        else:
+            m = np.asarray(mask, dtype=bool)
+            flags = np.zeros(n, dtype=np.int32)
+            flags[:m.size] = m
+        rows = fields.shape[0]
+        if flags[rows:].any():
+            raise ValueError("a selected member has no row in fields")
+        stride = fields[0].numel() if rows else 0
+        for k in np.flatnonzero(flags):
+            mdl = self._models[k]
+            if 3 * mdl.nx * mdl.nz > stride:
+                raise ValueError("fields rows are too short for member %d" % k)
+        torch.cuda.current_stream(fields.device).synchronize()
+        _capi.check(self._lib.psv_batch_set_parameter_fields_device(
+            self._h, ctypes.c_void_p(fields.data_ptr()), stride,
+            flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+
     def misfits(self):
         """L2 misfit of each member's model after forward() (float64, one per
         member in the order added; NaN for inactive members), equal bit for

@@ -362,6 +362,23 @@ void Batch::misfits(double *out, int n) {
   }
 }
 
+void Batch::set_parameter_fields_device(const double *fields, size_t member_stride,
+                                        const int *flags) {
+  if (!fields) throw Error(PSV_ERR_INVALID_ARGUMENT, "fields must not be NULL");
+  std::vector<const Model *> done;
+  for (size_t k = 0; k < members_.size(); ++k) {
+    if (flags && !flags[k]) continue;
+    Model *m = members_[k].first;
+    if (std::find(done.begin(), done.end(), m) != done.end()) continue;
+    done.push_back(m);
+    const size_t g = m->grid_size();
+    if (member_stride < 3 * g)
+      throw Error(PSV_ERR_INVALID_ARGUMENT, "member stride shorter than a member's fields");
+    const double *p = fields + k * member_stride;
+    m->set_parameter_fields(p, p + g, p + 2 * g, true);
+  }
+}
+
 int Batch::autotune(int n_steps) {
   if (members_.empty()) return tile_cfg_;
   // Every (launch scheme, tile shape) pair on n_steps steps of the members

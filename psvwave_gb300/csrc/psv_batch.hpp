@@ -40,6 +40,12 @@ class Batch {
   // batch's stream and one copy back; inactive members get NaN. Each active
   // model's misfit is updated as calculate_l2_misfit would.
   void misfits(double *out, int n);
+  // set_parameter_fields from device arrays for every member flagged
+  // non-zero in `flags` (all when null): member k's vp, vs and rho
+  // ([nx][nz] each, consecutive) start at fields + k * member_stride. A
+  // model that is a member more than once is set once. Each model queues
+  // its copies and medium update on its own stream as its own call does.
+  void set_parameter_fields_device(const double *fields, size_t member_stride, const int *flags);
   // Launch scheme: one launch per time step (false, the default) or every
   // step in one persistent launch over the tile table (true). A batch step
   // holds tens of thousands of tiles, many waves with no tail to recover,

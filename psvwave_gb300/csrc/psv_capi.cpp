@@ -671,6 +671,16 @@ int psv_batch_get_persistent(const psv_batch *b, int *persistent) {
   });
 }
 
+int psv_batch_set_parameter_fields_device(psv_batch *b, const double *fields,
+                                          long long member_stride, const int *flags) {
+  return guarded([&] {
+    need(b, "batch");
+    need(fields, "fields");
+    if (member_stride < 0) throw psv::Error(PSV_ERR_INVALID_ARGUMENT, "negative member stride");
+    b->impl.set_parameter_fields_device(fields, static_cast<size_t>(member_stride), flags);
+  });
+}
+
 int psv_batch_set_cluster(psv_batch *b, int cluster) {
   return guarded([&] {
     need(b, "batch");

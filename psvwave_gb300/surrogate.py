@@ -254,13 +254,12 @@ class FDPosterior:
         out = np.full(B, np.nan)
         if not sel.any():
             return out
-        # One wait for the fields; each model then only queues its copies
-        # and medium update (the batched forward waits for every member's
-        # stream, and `fields` lives until it returns).
+        # One wait for the fields and one call for every selected member;
+        # each model only queues its copies and medium update (the batched
+        # forward waits for every member's stream, and `fields` lives until
+        # it returns).
         fields = self.coarse.to_fields(z)
-        torch.cuda.current_stream(fields.device).synchronize()
-        for k in np.flatnonzero(sel):
-            self._set(k, fields[k], sync=False)
+        self.batch.set_parameter_fields_device(fields, sel)
         flags = np.zeros(len(self.models), dtype=bool)
         flags[:B] = sel
         self.batch.set_active(flags)

@@ -182,3 +182,42 @@ def test_batch_cluster_scheme_refused_for_large_members():
     if not b.cluster_fits:
         with pytest.raises(ValueError):
             b.cluster = True
+
+
+def test_batch_sets_member_media_from_one_device_tensor():
+    # One call sets the flagged members' media from rows of a device tensor:
+    # the same seismograms as each model's own set_parameter_fields.
+    import torch
+
+    models = cluster_models(nt=200)[:2] + cluster_models(nt=200)[:1]
+    shapes = {(m.nx, m.nz) for m in models}
+    assert len(shapes) == 1  # rows of one tensor
+    nx, nz = models[0].nx, models[0].nz
+    rng = np.random.default_rng(3)
+    media = []
+    for _ in models:
+        vp = 2000.0 * (1 + 0.05 * rng.standard_normal((nx, nz)))
+        media.append((vp, 0.45 * vp, np.full((nx, nz), 1600.0)))
+    ref = []
+    for m, md in zip(models, media):
+        m.kernel_variant = "fused_tma"
+        m.tile_shape = "20x28"
+        m.set_parameter_fields(*md)
+        m.forward_simulate(0, False)
+        ref.append([a.copy() for a in m.get_synthetic_data()])
+        m.set_parameter_fields(*[np.full((nx, nz), v) for v in (2000.0, 800.0, 1500.0)])
+    b = psv.Batch()
+    for m in models:
+        b.add(m, 0)
+    b.tile_shape = "20x28"
+    fields = torch.tensor(np.stack([np.stack(md) for md in media]), dtype=torch.float64,
+                          device="cuda")
+    b.set_parameter_fields_device(fields, [True, False, True])
+    b.forward()
+    for k, m in enumerate(models):
+        if k == 1:
+            assert np.allclose(m.get_parameter_fields()[0], 2000.0)
+            continue
+        ux, uz = m.get_synthetic_data()
+        assert np.array_equal(ux, ref[k][0]) and np.array_equal(uz, ref[k][1])
+        assert np.array_equal(m.get_parameter_fields()[0], media[k][0])
