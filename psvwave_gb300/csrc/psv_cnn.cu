@@ -1,13 +1,10 @@
 // Surrogate network kernels (forward, backward, Adam) and the coarse-to-grid
 // parameter map of the Monte Carlo workload; see psv_cnn.hpp.
 //
-// The forward convolutions and the weight gradients run on the tensor cores
-// (tcgen05 implicit GEMMs with BF16 hi + lo operand splits and FP32
-// accumulators in TMEM; see conv_forward_tc and conv_weight_tc). Input
-// gradients run one CTA per (sample, block of 8 input channels): the
-// sample's output gradients [cout][20 x 10] are staged in shared memory with
-// the block's BF16 weights, each of 200 threads computes one pixel with FP32
-// FMAs, and the next layer's ReLU mask is fused in. Weight gradients are
+// The convolutions run on the tensor cores as tcgen05 implicit GEMMs with
+// BF16 hi + lo operand splits and FP32 accumulators in TMEM: the forward
+// and the input gradient (with the ReLU mask of the layer's input fused in)
+// in conv_tc, the weight and bias gradients in conv_weight_tc as
 // fixed-order partial sums over position ranges that a second kernel adds
 // up, so every result is deterministic.
 #include "psv_cnn.hpp"
@@ -24,11 +21,9 @@ namespace cnn {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kBlk = 8;  // output (forward) or input (backward) channels per CTA
 
 size_t layer_size(int l) { return (size_t)kCout[l] * kCin[l] * 9 + kCout[l]; }
 
-size_t conv_smem() { return (size_t)kMaxC * kP * sizeof(float) + (size_t)kBlk * kMaxC * 9 * 2; }
 
 __device__ __forceinline__ void tap(int k, int dil, int &dh, int &dc) {
   dh = (k / 3 - 1) * dil;
@@ -103,13 +98,26 @@ __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
   return false;
 }
 
-template <bool RELU>
-__global__ void __launch_bounds__(kTcThreads) conv_forward_tc(int batch, int cin, int cout,
-                                                             int npad, int dil,
-                                                             const float *__restrict__ x,
-                                                             const __nv_bfloat16 *__restrict__ w,
-                                                             const float *__restrict__ bias,
-                                                             float *__restrict__ y, int *err) {
+// MODE kFwdRelu / kFwdLinear: the forward convolution above (x = layer
+// input [B][cin][kP], y = output [B][cout][kP], bias added, ReLU or not).
+// MODE kBwdData: the input gradient dx[b][ci][p] = (sum_co sum_tap
+// w[co][ci][tap] dy[b][co][p - off_tap]) [act[b][ci][p] > 0] as the same
+// implicit GEMM with the roles of the channels swapped: x = dy (gathered at
+// the negated tap offsets, K = cout * 9), B[ci][co * 9 + tap] =
+// w[co][ci][tap], N = cin rounded up to 16, and the ReLU mask of the
+// layer's input activation `act` applied in the epilogue (bias unused).
+constexpr int kFwdRelu = 0, kFwdLinear = 1, kBwdData = 2;
+
+template <int MODE>
+__global__ void __launch_bounds__(kTcThreads) conv_tc(int batch, int cin_l, int cout_l, int npad,
+                                                     int dil, const float *__restrict__ x,
+                                                     const __nv_bfloat16 *__restrict__ w,
+                                                     const float *__restrict__ bias,
+                                                     const float *__restrict__ act,
+                                                     float *__restrict__ y, int *err) {
+  constexpr bool BWD = MODE == kBwdData;
+  // Channels gathered (the GEMM's K / 9) and produced (its N).
+  const int cin = BWD ? cout_l : cin_l, cout = BWD ? cin_l : cout_l;
   __shared__ __align__(1024) unsigned char a_hi[kTcM * kTcKc * 2];
   __shared__ __align__(1024) unsigned char a_lo[kTcM * kTcKc * 2];
   __shared__ __align__(1024) unsigned char b_w[kTcCols * kTcKc * 2];
@@ -141,7 +149,7 @@ __global__ void __launch_bounds__(kTcThreads) conv_forward_tc(int batch, int cin
   for (int t = 0; t < 9; ++t) {
     int dh, dc;
     tap(t, dil, dh, dc);
-    const int hh = h + dh, cc = c + dc;
+    const int hh = BWD ? h - dh : h + dh, cc = BWD ? c - dc : c + dc;
     nb[t] = (row_ok && hh >= 0 && hh < kH && cc >= 0 && cc < kW) ? hh * kW + cc : -1;
   }
   const float *xb = x + (size_t)bs * cin * kP;
@@ -181,9 +189,13 @@ __global__ void __launch_bounds__(kTcThreads) conv_forward_tc(int batch, int cin
     }
     for (int i = tid; i < npad * kTcKc; i += kTcThreads) {
       const int co = i / kTcKc, kk = i - co * kTcKc, k = ci0 * 9 + kk;
-      const __nv_bfloat16 v = (co < cout && kk < 9 * kTcCi && k < K)
-                                  ? w[(size_t)co * K + k]
-                                  : __float2bfloat16_rn(0.f);
+      __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+      if (co < cout && kk < 9 * kTcCi && k < K) {
+        // Forward: w[co][k]. Input gradient: row co is the layer's input
+        // channel, k = (output channel, tap) of the layer.
+        v = BWD ? w[((size_t)(k / 9) * cout + co) * 9 + (k - 9 * (k / 9))]
+                : w[(size_t)co * K + k];
+      }
       *reinterpret_cast<__nv_bfloat16 *>(b_w + tc_off(co, kk)) = v;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -231,9 +243,14 @@ __global__ void __launch_bounds__(kTcThreads) conv_forward_tc(int batch, int cin
         for (int j = 0; j < 16; ++j) {
           const int co = c0 + j;
           if (co < cout) {
-            float r = __uint_as_float(v[j]) + bias[co];
-            if (RELU) r = fmaxf(r, 0.f);
-            y[((size_t)b * cout + co) * kP + p] = r;
+            const size_t o = ((size_t)b * cout + co) * kP + p;
+            if (BWD) {
+              y[o] = act[o] > 0.f ? __uint_as_float(v[j]) : 0.f;
+            } else {
+              float r = __uint_as_float(v[j]) + bias[co];
+              if (MODE == kFwdRelu) r = fmaxf(r, 0.f);
+              y[o] = r;
+            }
           }
         }
       }
@@ -414,63 +431,6 @@ __global__ void __launch_bounds__(kTcThreads) conv_weight_tc(int batch, int cin,
                  : "memory");
 }
 
-// dx[b][ci][p] = (sum_co sum_k w[co][ci][k] dy[b][co][p - off_k]) * [act[b][ci][p] > 0]
-__global__ void __launch_bounds__(kThreads) conv_backward_data(int cin, int cout, int dil,
-                                                               const float *__restrict__ dy,
-                                                               const __nv_bfloat16 *__restrict__ w,
-                                                               const float *__restrict__ act,
-                                                               float *__restrict__ dx) {
-  extern __shared__ float sm[];
-  float *ds = sm;                                                           // [cout][kP]
-  __nv_bfloat16 *ws = reinterpret_cast<__nv_bfloat16 *>(sm + kMaxC * kP);  // [kBlk][cout][9]
-  const int b = blockIdx.x, ci0 = blockIdx.y * kBlk;
-  const int nci = min(kBlk, cin - ci0);
-  const float *db = dy + (size_t)b * cout * kP;
-  for (int i = threadIdx.x; i < cout * kP; i += blockDim.x) ds[i] = db[i];
-  for (int i = threadIdx.x; i < nci * cout * 9; i += blockDim.x) {
-    const int ci = i / (cout * 9), r = i - ci * cout * 9, co = r / 9, k = r - co * 9;
-    ws[i] = w[((size_t)co * cin + ci0 + ci) * 9 + k];
-  }
-  __syncthreads();
-  const int p = threadIdx.x;
-  if (p >= kP) return;
-  const int h = p / kW, c = p - h * kW;
-  int nb[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    int dh, dc;
-    tap(k, dil, dh, dc);
-    const int hh = h - dh, cc = c - dc;
-    nb[k] = (hh >= 0 && hh < kH && cc >= 0 && cc < kW) ? hh * kW + cc : -1;
-  }
-  float acc[kBlk];
-#pragma unroll
-  for (int o = 0; o < kBlk; ++o) acc[o] = 0.f;
-  for (int co = 0; co < cout; ++co) {
-    const float *dr = ds + co * kP;
-    float v[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) v[k] = nb[k] >= 0 ? dr[nb[k]] : 0.f;
-#pragma unroll
-    for (int o = 0; o < kBlk; ++o) {
-      if (o < nci) {
-        const __nv_bfloat16 *wr = ws + (o * cout + co) * 9;
-        float a = acc[o];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) a = fmaf(__bfloat162float(wr[k]), v[k], a);
-        acc[o] = a;
-      }
-    }
-  }
-#pragma unroll
-  for (int o = 0; o < kBlk; ++o) {
-    if (o < nci) {
-      const size_t i = ((size_t)b * cin + ci0 + o) * kP + p;
-      dx[i] = act[i] > 0.f ? acc[o] : 0.f;
-    }
-  }
-}
-
 __global__ void sum_chunks(size_t len, const float *__restrict__ partial, float *__restrict__ out) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= len) return;
@@ -568,16 +528,6 @@ unsigned blocks(size_t n, int t = 256) { return static_cast<unsigned>((n + t - 1
 
 void check(cudaError_t e, const char *what) { cuda_check(e, what); }
 
-void configure_once(int device) {
-  static unsigned long long done = 0;
-  const unsigned long long bit = 1ull << (device & 63);
-  if (done & bit) return;
-  const int smem = static_cast<int>(conv_smem());
-  check(cudaFuncSetAttribute(conv_backward_data, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
-        "conv smem");
-  done |= bit;
-}
-
 }  // namespace
 
 size_t weight_offset(int layer) {
@@ -594,7 +544,6 @@ Net::Net(int device, int max_batch) : device_(device), max_batch_(max_batch) {
   if (max_batch <= 0) throw Error(PSV_ERR_INVALID_ARGUMENT, "max_batch must be positive");
   DeviceGuard guard(device_);
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
-  configure_once(device_);
   const size_t n = num_params();
   params_.allocate(n * sizeof(float));
   wbf_.allocate(n * sizeof(__nv_bfloat16));
@@ -676,11 +625,11 @@ void Net::forward(int batch, const float *x) {
     const int npad = std::max(16, (kCout[l] + 15) / 16 * 16);
     const unsigned tiles = static_cast<unsigned>((batch * kP + kTcM - 1) / kTcM);
     if (l + 1 < kLayers)
-      conv_forward_tc<true><<<tiles, kTcThreads, 0, stream_>>>(
-          batch, kCin[l], kCout[l], npad, kDil[l], in, w, bias, out, err_.as<int>());
+      conv_tc<kFwdRelu><<<tiles, kTcThreads, 0, stream_>>>(
+          batch, kCin[l], kCout[l], npad, kDil[l], in, w, bias, nullptr, out, err_.as<int>());
     else
-      conv_forward_tc<false><<<tiles, kTcThreads, 0, stream_>>>(
-          batch, kCin[l], kCout[l], npad, kDil[l], in, w, bias, out, err_.as<int>());
+      conv_tc<kFwdLinear><<<tiles, kTcThreads, 0, stream_>>>(
+          batch, kCin[l], kCout[l], npad, kDil[l], in, w, bias, nullptr, out, err_.as<int>());
     check(cudaGetLastError(), "conv forward");
     in = out;
   }
@@ -688,7 +637,6 @@ void Net::forward(int batch, const float *x) {
 
 double Net::backward(int batch, const float *x, const float *m_true, const float *g_true,
                      float w_misfit, float w_grad) {
-  const size_t smem = conv_smem();
   float *cur = dact_[0].as<float>(), *other = dact_[1].as<float>();
   head_loss<<<batch, kThreads, 0, stream_>>>(batch, act_[kLayers - 1].as<float>(), m_true, g_true,
                                              w_misfit, w_grad, cur, loss_partials_.as<double>());
@@ -706,10 +654,11 @@ double Net::backward(int batch, const float *x, const float *m_true, const float
                                                  grads_.as<float>() + weight_offset(l));
     check(cudaGetLastError(), "conv backward weight");
     if (l > 0) {
-      const dim3 grid(batch, (kCin[l] + kBlk - 1) / kBlk);
-      conv_backward_data<<<grid, kThreads, smem, stream_>>>(
-          kCin[l], kCout[l], kDil[l], cur, wbf_.as<__nv_bfloat16>() + weight_offset(l),
-          act_[l - 1].as<float>(), other);
+      const unsigned tiles = static_cast<unsigned>((batch * kP + kTcM - 1) / kTcM);
+      conv_tc<kBwdData><<<tiles, kTcThreads, 0, stream_>>>(
+          batch, kCin[l], kCout[l], std::max(16, (kCin[l] + 15) / 16 * 16), kDil[l], cur,
+          wbf_.as<__nv_bfloat16>() + weight_offset(l), nullptr, act_[l - 1].as<float>(), other,
+          err_.as<int>());
       check(cudaGetLastError(), "conv backward data");
       std::swap(cur, other);
     }
