@@ -30,7 +30,7 @@ __device__ __forceinline__ void tap(int k, int dil, int &dh, int &dc) {
   dc = (k % 3 - 1) * dil;
 }
 
-// ---- tensor-core forward convolution (tcgen05) ---------------------------
+// ---- tensor-core convolutions (tcgen05): forward and input gradient -------
 //
 // The forward convolution as an implicit GEMM on the 5th-generation tensor
 // cores: D[pos][co] = sum_k A[pos][k] W[co][k], with pos = b kP + p running
