@@ -2,7 +2,7 @@
 one-rank NCCL group on one GPU: the device-resident all-reduce of
 sharded_gradient (kernels from the solver's device buffers, CUDA tensors
 back), the batched runner of sharded_forward, and sharded_da_hmc over the
-real solver judge all give what one process gives. The multi-rank splits
+real solver judge (NCCL object gathers) all give what one process gives. The multi-rank splits
 themselves are covered by the gloo tests (tests/test_distributed.py); a box
 here has one GPU."""
 import os
@@ -80,3 +80,23 @@ def test_sharded_forward_batch_runner(nccl_group):
             m.forward_simulate(s, False)
         rx, rz = m.get_synthetic_data()
         assert np.array_equal(ux, rx) and np.array_equal(uz, rz)
+
+
+def test_sharded_da_hmc_matches_one_process(nccl_group):
+    from psvwave_gb300 import surrogate as sg
+
+    S = sg.c4_setup(4, s2=1.0)
+    post = S["posterior"]
+    post.s2 = float(post.misfits(torch.zeros((1, 3, 20, 10), device="cuda"))[0]) / 20.0
+    net = sg.SurrogateNet(max_batch=64, seed=2)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(3)
+    z0 = 0.5 * torch.randn((4, 3, 20, 10), device="cuda", generator=gen)
+    kw = dict(screen=0.5, force=0.0)
+    got = distributed.sharded_da_hmc(post, net, z0, 3, 0.03, 4, seed=7, group=nccl_group, **kw)
+    want = sg.da_hmc(post, net, z0, 3, 0.03, 4, seed=7, **kw)
+    assert got["proposals"] == want["proposals"] == 12
+    assert got["stage1_accepted"] == want["stage1_accepted"]
+    assert got["accepted"] == want["accepted"]
+    assert torch.equal(got["samples"], want["samples"].cpu())
+    assert torch.equal(got["z"], want["z"].cpu())
