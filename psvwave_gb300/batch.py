@@ -1,6 +1,9 @@
 """Batched forward simulation: shots of many fdModels, of uneven grid sizes,
-advanced together in one TMA-step launch per time step with the whole time
-loop replayed as one CUDA graph (C ABI psv_batch_*)."""
+advanced together (C ABI psv_batch_*): one TMA-step launch per time step
+with the whole time loop replayed as one CUDA graph (the default), every
+step in one persistent launch, or every member in its own cluster-resident
+launch; the autotuner picks. Media updates and misfits of many members go
+through one call each."""
 import ctypes
 
 from . import _capi
